@@ -1,0 +1,226 @@
+/*
+ * ptgpu.h -- C ABI of the GB300 (sm_103a) LBVH builder and path tracer.
+ *
+ * This header is the drop-in boundary for PTGPU_PC's hot path: the LBVH build
+ * (CLBVH + BVH.cl), the host KD-tree build (KDTree.cpp), the scene loader
+ * (displayfunc.cpp Read/ReadTxt/ReadScene, UpdateCamera) and the per-pixel
+ * radiance path tracer (rendering_kernel.cl RadianceGPU).  Every struct below
+ * keeps the byte layout of the reference struct it mirrors (checked by the
+ * static asserts at the end), so arrays produced by the reference can be passed
+ * in unchanged and arrays returned here can be handed to reference code.
+ *
+ * Conventions
+ *  - Every function returns an int status: PTGPU_OK (0) or a negative
+ *    PTGPU_E_* code.  ptgpu_status_string() names it; ptgpu_last_error()
+ *    gives a one-line message for the last failure on the calling thread.
+ *  - Host pointers only; no CUDA or torch types in any signature.  Device
+ *    memory is owned by the context.  A stream may be supplied as an opaque
+ *    handle (cudaStream_t cast to void*) through ptgpu_config.stream.
+ *  - One context per thread.  Device-side waits are bounded and surface as
+ *    PTGPU_E_TIMEOUT; the context stays usable afterwards.
+ */
+#ifndef PTGPU_H
+#define PTGPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTGPU_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+#define PTGPU_OK           0
+#define PTGPU_E_INVAL     -1  /* bad argument, bad count, unsupported mode      */
+#define PTGPU_E_OOM       -2  /* device or host allocation failed               */
+#define PTGPU_E_DEVICE    -3  /* CUDA error (sticky errors need a new context)  */
+#define PTGPU_E_TIMEOUT   -4  /* a bounded device wait gave up                  */
+#define PTGPU_E_IO        -5  /* scene file missing or malformed                */
+#define PTGPU_E_RANGE     -6  /* result does not fit the reference layout       */
+#define PTGPU_E_STATE     -7  /* call out of order (e.g. draw before build)     */
+
+/* ---- reference constants (include/geom.h:29-35, clheader.h:9-15) --------- */
+#define PTGPU_EPSILON      0.01f
+#define PTGPU_MAX_DEPTH    6
+#define PTGPU_ACCEL_NONE   0   /* ACCELSTR 0: brute force                   */
+#define PTGPU_ACCEL_BVH    1   /* ACCELSTR 1: LBVH (the reference default)  */
+#define PTGPU_ACCEL_KDTREE 2   /* ACCELSTR 2: host-built KD tree            */
+
+/* ---- shared geometry types (include/geom.h:48-91, vec.h:27-29) ----------- */
+typedef struct { float x, y, z; } ptgpu_vec;                 /* Vec      */
+typedef struct { ptgpu_vec o, d; } ptgpu_ray;                /* Ray      */
+typedef struct { float rad; ptgpu_vec p; } ptgpu_sphere;     /* Sphere   */
+typedef struct { ptgpu_vec p1, p2, p3; } ptgpu_triangle;     /* Triangle */
+typedef struct {                                             /* Bound    */
+    float min_x, max_x, min_y, max_y, min_z, max_z;
+} ptgpu_bound;
+
+enum { PTGPU_SPHERE = 0, PTGPU_TRIANGLE = 1 };            /* tagType     */
+enum { PTGPU_DIFF = 0, PTGPU_SPEC = 1, PTGPU_REFR = 2 };  /* enum Refl   */
+
+typedef struct {                                             /* Shape    */
+    int32_t type;                 /* PTGPU_SPHERE / PTGPU_TRIANGLE  @0  */
+    union { ptgpu_triangle t; ptgpu_sphere s; } g;       /*          @4  */
+    ptgpu_vec e, c;               /* emission @40, colour @52             */
+    int32_t refl;                 /* PTGPU_DIFF/SPEC/REFR           @64 */
+    int32_t index;                /*                                @68 */
+    uint32_t morton_code;         /*                                @72 */
+    ptgpu_bound b;                /*                                @76 */
+    float area;                   /*                                @100*/
+} ptgpu_shape;
+
+/* include/camera.h:29-38 */
+typedef struct {
+    ptgpu_vec orig, target;       /* target is read but unused (UpdateCamera) */
+    float pitch, yaw;
+    float width, height;
+    ptgpu_vec dir, x, y;          /* filled by ptgpu_update_camera */
+} ptgpu_camera;
+
+/* include/BVHNodeGPU.h:4-16.  btn[N-1] internal nodes, btl[N] leaves. */
+typedef struct {
+    int32_t min, max;             /* leaf range of an internal node         */
+    int32_t nShape;               /* shape id (leaves)                      */
+    int32_t leaf;                 /* 0 internal, 2 "has a leaf child", -1 leaf */
+    int32_t nLeft, nRight, nParent;
+    ptgpu_bound bound;
+    float cost, area;
+} ptgpu_bvh_node;
+
+/* include/KDNodeGPU.h:4-14.  Heap layout, root at index 1. */
+typedef struct {
+    int16_t leaf;
+    int16_t nLeft, nRight, nParent;
+    ptgpu_bound bound;
+    int16_t min, max;             /* [min,max) into the kn index list       */
+} ptgpu_kd_node;
+
+/* ---- context -------------------------------------------------------------- */
+typedef struct ptgpu_ctx ptgpu_ctx;
+
+typedef struct {
+    int32_t device;        /* CUDA device ordinal                               */
+    int32_t accel;         /* PTGPU_ACCEL_*: runtime form of ACCELSTR           */
+    int32_t max_depth;     /* MAX_DEPTH; 0 selects the reference value 6        */
+    int32_t width, height; /* image size; sets camera.width/height              */
+    int32_t block_size;    /* render block size; 0 = default                    */
+    int32_t flags;         /* PTGPU_FLAG_*                                       */
+    int32_t reserved;
+    void   *stream;        /* optional cudaStream_t; NULL = context-owned stream */
+} ptgpu_config;
+
+/* build / render flags */
+#define PTGPU_FLAG_WAVEFRONT     0x1  /* render with the queue-based wavefront  */
+#define PTGPU_FLAG_MORTON_DELTA  0x2  /* Karras split on Morton keys (quality)  */
+#define PTGPU_FLAG_TREELET       0x4  /* treelet reoptimisation after refit     */
+#define PTGPU_FLAG_ARGS_RTL      0x8  /* draw the two randoms of a light sample
+                                         right-to-left (the order g++ gives the
+                                         reference source; the default is the
+                                         left-to-right order of OpenCL/clang)   */
+
+int  ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out);
+int  ptgpu_destroy(ptgpu_ctx *ctx);
+const char *ptgpu_status_string(int status);
+const char *ptgpu_last_error(void);
+int  ptgpu_abi_version(void);
+
+/* ---- scene ---------------------------------------------------------------- */
+/* Read(fileName, &walllight) + AddWallLight (displayfunc.cpp:717-730,
+ * smallptGPU.cpp:1448-1459): ".txt", ".scn" dispatch by extension.  Sets the
+ * context's shapes, light count and camera (orig/target, pitch=yaw=0).        */
+int  ptgpu_read_scene(ptgpu_ctx *ctx, const char *path, int32_t *walllight);
+/* Copies n shapes in (the global `shapes`/`shapeCnt`/`lightCnt`). */
+int  ptgpu_set_shapes(ptgpu_ctx *ctx, const ptgpu_shape *shapes, uint32_t n,
+                      uint32_t light_cnt);
+int  ptgpu_get_shape_count(ptgpu_ctx *ctx, uint32_t *n, uint32_t *light_cnt);
+/* Copies the shapes out; after a BVH build index/morton_code/b are filled
+ * as CLBVH::CLBVH leaves them (CLBVH.cpp:98-164). */
+int  ptgpu_get_shapes(ptgpu_ctx *ctx, ptgpu_shape *out, uint32_t n);
+
+/* UpdateCamera (displayfunc.cpp:732-756): pure host function. */
+int  ptgpu_update_camera(ptgpu_camera *cam);
+/* Sets the render camera; width/height are forced to the context's size and
+ * the basis is recomputed with ptgpu_update_camera (ReInit semantics). */
+int  ptgpu_set_camera(ptgpu_ctx *ctx, const ptgpu_camera *cam);
+int  ptgpu_get_camera(ptgpu_ctx *ctx, ptgpu_camera *cam);
+
+/* ---- acceleration structures ---------------------------------------------- */
+/* BuildBVH (smallptGPU.cpp:1462-1472) or BuildKDtree (:1477-1493). */
+int  ptgpu_build(ptgpu_ctx *ctx, int32_t accel, uint32_t flags);
+/* CLBVH::getTrees (CLBVH.cpp:357-366): copies btn[N-1] and btl[N] out. */
+int  ptgpu_get_bvh(ptgpu_ctx *ctx, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl);
+/* KDTree::getTrees (KDTree.cpp:257-270).  Size query: pass NULL buffers to
+ * get *kng_cnt / *kn_cnt.  PTGPU_E_RANGE if the heap overflows int16. */
+int  ptgpu_get_kdtree(ptgpu_ctx *ctx, ptgpu_kd_node *kng, int32_t *kng_cnt,
+                      int32_t *kn, int32_t *kn_cnt);
+/* Installs caller-built BVH arrays (the ReInit upload, smallptGPU.cpp:1145-1148). */
+int  ptgpu_set_bvh(ptgpu_ctx *ctx, const ptgpu_bvh_node *btn,
+                   const ptgpu_bvh_node *btl, uint32_t n);
+/* Last build's device time in milliseconds (CUDA events on the ctx stream). */
+int  ptgpu_last_build_ms(ptgpu_ctx *ctx, float *ms);
+
+/* ---- rendering ------------------------------------------------------------ */
+/* Seeds: 2*W*H words, seed0/seed1 interleaved per pixel (AllocateBuffers,
+ * smallptGPU.cpp:185-217).  ptgpu_make_seeds fills them from a 64-bit master
+ * seed (SplitMix64, low 32 bits, clamped to >= 2 like the reference). */
+int  ptgpu_make_seeds(uint64_t master_seed, uint32_t *seeds, uint32_t count);
+int  ptgpu_set_seeds(ptgpu_ctx *ctx, const uint32_t *seeds);
+int  ptgpu_get_seeds(ptgpu_ctx *ctx, uint32_t *seeds);
+/* Resets the progressive sample counter (ReInit: currentSample = 0). */
+int  ptgpu_reset_accumulation(ptgpu_ctx *ctx);
+/* DrawFrame (smallptGPU.cpp:918-1126): runs `passes` RadianceGPU passes and
+ * returns the RGBA8 pixel buffer (library-owned, valid until the next call). */
+int  ptgpu_draw_frame(ptgpu_ctx *ctx, uint32_t passes, const uint32_t **pixels_out);
+/* Enqueues `passes` passes without any host copy (device-resident timing). */
+int  ptgpu_render_async(ptgpu_ctx *ctx, uint32_t passes);
+int  ptgpu_synchronize(ptgpu_ctx *ctx);
+/* The float accumulation buffer `colors` (W*H Vec, row-flipped as in
+ * RadianceGPU) and the packed pixels. */
+int  ptgpu_get_colors(ptgpu_ctx *ctx, ptgpu_vec *colors);
+int  ptgpu_get_pixels(ptgpu_ctx *ctx, uint32_t *pixels);
+int  ptgpu_get_current_sample(ptgpu_ctx *ctx, int32_t *current_sample);
+
+/* ---- closest-hit queries ---------------------------------------------------- */
+/* Intersect (rendering_kernel.cl:194-363) for n rays with the current accel:
+ * t[i] (1e20 on a miss), id[i] (shape id), hit[i] (0/1). */
+int  ptgpu_trace_closest(ptgpu_ctx *ctx, const ptgpu_ray *rays, uint32_t n,
+                         float *t, uint32_t *id, int32_t *hit);
+
+/* Device-resident variants for benchmarking: the arrays live in memory the
+ * caller allocated with CUDA on the context's device. */
+int  ptgpu_trace_closest_device(ptgpu_ctx *ctx, const ptgpu_ray *d_rays,
+                                uint32_t n, float *d_t, uint32_t *d_id,
+                                int32_t *d_hit);
+int  ptgpu_get_stream(ptgpu_ctx *ctx, void **stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+/* ---- layout checks against the reference structs -------------------------- */
+#ifdef __cplusplus
+#define PTGPU_SA(c, m) static_assert(c, m)
+#else
+#define PTGPU_SA(c, m) _Static_assert(c, m)
+#endif
+PTGPU_SA(sizeof(ptgpu_vec) == 12, "Vec is 12 bytes");
+PTGPU_SA(sizeof(ptgpu_ray) == 24, "Ray is 24 bytes");
+PTGPU_SA(sizeof(ptgpu_sphere) == 16, "Sphere is 16 bytes");
+PTGPU_SA(sizeof(ptgpu_triangle) == 36, "Triangle is 36 bytes");
+PTGPU_SA(sizeof(ptgpu_bound) == 24, "Bound is 24 bytes");
+PTGPU_SA(sizeof(ptgpu_shape) == 104, "Shape is 104 bytes");
+PTGPU_SA(offsetof(ptgpu_shape, e) == 40, "Shape.e at 40");
+PTGPU_SA(offsetof(ptgpu_shape, refl) == 64, "Shape.refl at 64");
+PTGPU_SA(offsetof(ptgpu_shape, morton_code) == 72, "Shape.morton_code at 72");
+PTGPU_SA(offsetof(ptgpu_shape, b) == 76, "Shape.b at 76");
+PTGPU_SA(offsetof(ptgpu_shape, area) == 100, "Shape.area at 100");
+PTGPU_SA(sizeof(ptgpu_camera) == 76, "Camera is 76 bytes");
+PTGPU_SA(sizeof(ptgpu_bvh_node) == 60, "BVHNodeGPU is 60 bytes");
+PTGPU_SA(offsetof(ptgpu_bvh_node, bound) == 28, "BVHNodeGPU.bound at 28");
+PTGPU_SA(sizeof(ptgpu_kd_node) == 36, "KDNodeGPU is 36 bytes");
+PTGPU_SA(offsetof(ptgpu_kd_node, min) == 32, "KDNodeGPU.min at 32");
+#undef PTGPU_SA
+
+#endif /* PTGPU_H */

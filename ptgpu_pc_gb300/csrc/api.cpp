@@ -1,0 +1,645 @@
+// api.cpp -- the C ABI (include/ptgpu.h): context, scene, builds, rendering.
+//
+// The context replaces the reference's process globals (smallptGPU.cpp:108-
+// 119, displayfunc.cpp:85-98): shapes, light count, camera, seeds, the
+// accumulation buffer and the acceleration structure all live in one object
+// that owns its device memory and stream.
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "host.h"
+#include "lbvh.h"
+
+using namespace ptgpu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    int code = (e == cudaErrorMemoryAllocation) ? PTGPU_E_OOM : PTGPU_E_DEVICE;
+    return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (expr);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);        \
+    } while (0)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (want == 0) want = 16;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+bool viszero(const ptgpu_vec &v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
+
+}  // namespace
+
+struct ptgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 1;
+    int max_depth = PTGPU_MAX_DEPTH;
+    int accel_cfg = PTGPU_ACCEL_BVH;
+    int block = 128;
+    int flags = 0;
+    // scene
+    std::vector<ptgpu_shape> h_shapes;
+    uint32_t n = 0, light_cnt = 0;
+    int n_lights = 0;
+    bool all_tri = true;
+    DevBuf d_shapes, d_verts, d_type, d_prims0, d_mats, d_lights;
+    bool shapes_exported = false;
+    // acceleration structure
+    int accel_built = -1;
+    bool bvh_valid = false;
+    DevBuf d_btn, d_btl, d_keys, d_keys_alt, d_keys_tmp, d_vals_alt, d_vals_tmp, d_sorted;
+    DevBuf d_status, d_state, d_tile_bounds;
+    DevBuf d_nodes, d_prims, d_prim_id, d_root_box, d_identity;
+    int32_t root_first = 0, root_count = 0;
+    KdTree kd;
+    bool kd_valid = false;
+    // rendering
+    int w = 0, h = 0;
+    DevBuf d_colors, d_pixels, d_seeds, d_err;
+    uint32_t *h_pixels = nullptr;
+    int current_sample = 0;
+    ptgpu_camera cam{};
+    bool cam_set = false;
+    // queries
+    DevBuf d_rays, d_t, d_id, d_hit;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_build_ms = 0.f;
+    int rtl = 0;
+};
+
+static TraceView make_view(ptgpu_ctx *c) {
+    TraceView tv;
+    std::memset(&tv, 0, sizeof(tv));
+    tv.n_shapes = (int32_t)c->n;
+    tv.error_flags = c->d_err.as<int32_t>();
+    if (c->accel_built == PTGPU_ACCEL_NONE || (c->accel_built == PTGPU_ACCEL_BVH && c->n == 1)) {
+        tv.accel = PTGPU_ACCEL_NONE;
+        tv.prims = c->d_prims0.as<float4>();
+        tv.prim_id = c->d_identity.as<int32_t>();
+        return tv;
+    }
+    tv.accel = c->accel_built;
+    tv.nodes = c->d_nodes.as<float4>();
+    tv.prims = c->d_prims.as<float4>();
+    tv.prim_id = c->d_prim_id.as<int32_t>();
+    tv.root_first = c->root_first;
+    tv.root_count = c->root_count;
+    tv.root_box = c->d_root_box.as<float>();
+    return tv;
+}
+
+extern "C" {
+
+int ptgpu_abi_version(void) { return PTGPU_ABI_VERSION; }
+
+const char *ptgpu_last_error(void) { return g_last_error.c_str(); }
+
+const char *ptgpu_status_string(int s) {
+    switch (s) {
+    case PTGPU_OK: return "ok";
+    case PTGPU_E_INVAL: return "invalid argument";
+    case PTGPU_E_OOM: return "out of memory";
+    case PTGPU_E_DEVICE: return "device error";
+    case PTGPU_E_TIMEOUT: return "device wait timed out";
+    case PTGPU_E_IO: return "scene i/o error";
+    case PTGPU_E_RANGE: return "result does not fit the reference layout";
+    case PTGPU_E_STATE: return "call out of order";
+    default: return "unknown status";
+    }
+}
+
+int ptgpu_make_seeds(uint64_t master, uint32_t *seeds, uint32_t count) {
+    if (!seeds && count) return fail(PTGPU_E_INVAL, "null seed buffer");
+    make_seeds(master, seeds, count);
+    return PTGPU_OK;
+}
+
+int ptgpu_update_camera(ptgpu_camera *cam) {
+    if (!cam) return fail(PTGPU_E_INVAL, "null camera");
+    update_camera(cam);
+    return PTGPU_OK;
+}
+
+int ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out) {
+    if (!cfg || !out) return fail(PTGPU_E_INVAL, "null config or output");
+    if (cfg->width <= 0 || cfg->height <= 0 || (int64_t)cfg->width * cfg->height > (1ll << 30))
+        return fail(PTGPU_E_INVAL, "width and height must be positive");
+    if (cfg->accel < 0 || cfg->accel > 2) return fail(PTGPU_E_INVAL, "accel must be 0, 1 or 2");
+    if (cfg->max_depth < 0 || cfg->max_depth > 1024) return fail(PTGPU_E_INVAL, "bad max_depth");
+    *out = nullptr;
+    ptgpu_ctx *c = new ptgpu_ctx();
+    c->device = cfg->device;
+    c->accel_cfg = cfg->accel;
+    c->max_depth = cfg->max_depth ? cfg->max_depth : PTGPU_MAX_DEPTH;
+    c->block = cfg->block_size > 0 ? cfg->block_size : 128;
+    c->flags = cfg->flags;
+    c->rtl = (cfg->flags & PTGPU_FLAG_ARGS_RTL) ? 1 : 0;
+    c->w = cfg->width;
+    c->h = cfg->height;
+    auto bail = [&](int code) { ptgpu_destroy(c); return code; };
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+    if (cfg->stream) {
+        c->stream = (cudaStream_t)cfg->stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+        c->own_stream = true;
+    }
+    if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
+    if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
+    const size_t npx = (size_t)c->w * c->h;
+    if ((e = c->d_colors.ensure(npx * sizeof(ptgpu_vec))) != cudaSuccess) return bail(cuda_fail(e, "alloc colors"));
+    if ((e = c->d_pixels.ensure(npx * sizeof(uint32_t))) != cudaSuccess) return bail(cuda_fail(e, "alloc pixels"));
+    if ((e = c->d_seeds.ensure(npx * 2 * sizeof(uint32_t))) != cudaSuccess) return bail(cuda_fail(e, "alloc seeds"));
+    if ((e = c->d_err.ensure(16)) != cudaSuccess) return bail(cuda_fail(e, "alloc error word"));
+    if ((e = cudaMallocHost(&c->h_pixels, npx * sizeof(uint32_t))) != cudaSuccess)
+        return bail(cuda_fail(e, "alloc pinned pixels"));
+    cudaMemsetAsync(c->d_err.p, 0, 16, c->stream);
+    cudaMemsetAsync(c->d_colors.p, 0, npx * sizeof(ptgpu_vec), c->stream);
+    std::vector<uint32_t> seeds(npx * 2);
+    make_seeds(1, seeds.data(), (uint32_t)seeds.size());
+    e = cudaMemcpyAsync(c->d_seeds.p, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "upload seeds"));
+    *out = c;
+    return PTGPU_OK;
+}
+
+int ptgpu_destroy(ptgpu_ctx *c) {
+    if (!c) return PTGPU_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->d_shapes, &c->d_verts, &c->d_type, &c->d_prims0, &c->d_mats, &c->d_lights,
+                      &c->d_btn, &c->d_btl, &c->d_keys, &c->d_keys_alt, &c->d_keys_tmp, &c->d_vals_alt,
+                      &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_tile_bounds,
+                      &c->d_nodes, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
+                      &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_rays, &c->d_t,
+                      &c->d_id, &c->d_hit};
+    for (DevBuf *b : bufs) b->release();
+    if (c->h_pixels) cudaFreeHost(c->h_pixels);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_stream(ptgpu_ctx *c, void **stream) {
+    if (!c || !stream) return fail(PTGPU_E_INVAL, "null argument");
+    *stream = (void *)c->stream;
+    return PTGPU_OK;
+}
+
+int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt) {
+    if (!c || (!shapes && n)) return fail(PTGPU_E_INVAL, "null argument");
+    if (n == 0) return fail(PTGPU_E_INVAL, "a scene needs at least one shape");
+    if (n >= (1u << 30)) return fail(PTGPU_E_INVAL, "too many shapes (limit 2^30-1)");
+    for (uint32_t i = 0; i < n; ++i)
+        if (shapes[i].type != PTGPU_SPHERE && shapes[i].type != PTGPU_TRIANGLE)
+            return fail(PTGPU_E_INVAL, "shape " + std::to_string(i) + " has an unknown type");
+    cudaSetDevice(c->device);
+    c->h_shapes.assign(shapes, shapes + n);
+    c->n = n;
+    c->light_cnt = light_cnt;
+    c->all_tri = true;
+    for (uint32_t i = 0; i < n; ++i) if (shapes[i].type != PTGPU_TRIANGLE) { c->all_tri = false; break; }
+    // emitters visited by SampleLights: the first light_cnt in index order
+    std::vector<LightRec> lights;
+    for (uint32_t i = 0; i < n && lights.size() < light_cnt; ++i) {
+        const ptgpu_shape &s = shapes[i];
+        if (viszero(s.e)) continue;
+        LightRec L;
+        std::memset(&L, 0, sizeof(L));
+        if (s.type == PTGPU_TRIANGLE) {
+            const ptgpu_triangle &t = s.g.t;
+            int32_t tt = PTGPU_TRIANGLE; float tf; std::memcpy(&tf, &tt, 4);
+            L.a = make_float4(t.p1.x, t.p1.y, t.p1.z, tf);
+            L.b = make_float4(t.p2.x - t.p1.x, t.p2.y - t.p1.y, t.p2.z - t.p1.z, s.area);
+            L.c = make_float4(t.p3.x - t.p1.x, t.p3.y - t.p1.y, t.p3.z - t.p1.z, 0.f);
+        } else {
+            int32_t tt = PTGPU_SPHERE; float tf; std::memcpy(&tf, &tt, 4);
+            L.a = make_float4(s.g.s.p.x, s.g.s.p.y, s.g.s.p.z, tf);
+            L.b = make_float4(s.g.s.rad, 0.f, 0.f, s.area);
+        }
+        L.e = make_float4(s.e.x, s.e.y, s.e.z, 0.f);
+        lights.push_back(L);
+    }
+    c->n_lights = (int)lights.size();
+    CK(c->d_shapes.ensure((size_t)n * sizeof(ptgpu_shape)));
+    CK(c->d_verts.ensure((size_t)n * 9 * sizeof(float)));
+    CK(c->d_type.ensure((size_t)n));
+    CK(c->d_prims0.ensure((size_t)n * 3 * sizeof(float4)));
+    CK(c->d_mats.ensure((size_t)n * sizeof(Material)));
+    CK(c->d_lights.ensure(lights.size() * sizeof(LightRec)));
+    CK(c->d_identity.ensure((size_t)n * sizeof(int32_t)));
+    std::vector<int32_t> ident(n);
+    for (uint32_t i = 0; i < n; ++i) ident[i] = (int32_t)i;
+    CK(cudaMemcpyAsync(c->d_shapes.p, shapes, (size_t)n * sizeof(ptgpu_shape), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_identity.p, ident.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    if (!lights.empty())
+        CK(cudaMemcpyAsync(c->d_lights.p, lights.data(), lights.size() * sizeof(LightRec), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_unpack_shapes(c->d_shapes.as<ptgpu_shape>(), (int)n, c->d_verts.as<float>(),
+                            c->d_type.as<uint8_t>(), c->d_prims0.as<float4>(), c->d_mats.as<Material>(),
+                            c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->accel_built = -1;
+    c->bvh_valid = false;
+    c->kd_valid = false;
+    c->shapes_exported = false;
+    c->current_sample = 0;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_shape_count(ptgpu_ctx *c, uint32_t *n, uint32_t *light_cnt) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    if (n) *n = c->n;
+    if (light_cnt) *light_cnt = c->light_cnt;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_shapes(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
+    if (!c || !out) return fail(PTGPU_E_INVAL, "null argument");
+    if (n != c->n) return fail(PTGPU_E_INVAL, "shape count mismatch");
+    if (c->accel_built == PTGPU_ACCEL_BVH && c->bvh_valid && c->d_keys.p) {
+        cudaSetDevice(c->device);
+        if (!c->shapes_exported) {
+            CK(launch_export_shapes(c->d_shapes.as<ptgpu_shape>(), c->d_verts.as<float>(),
+                                    c->d_type.as<uint8_t>(), c->d_keys.as<uint32_t>(), (int)n, c->stream));
+            c->shapes_exported = true;
+        }
+        CK(cudaMemcpyAsync(out, c->d_shapes.p, (size_t)n * sizeof(ptgpu_shape), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return PTGPU_OK;
+    }
+    std::memcpy(out, c->h_shapes.data(), (size_t)n * sizeof(ptgpu_shape));
+    return PTGPU_OK;
+}
+
+int ptgpu_read_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
+    if (!c || !path) return fail(PTGPU_E_INVAL, "null argument");
+    LoadedScene sc;
+    std::string err;
+    int st = read_scene(path, c->w, c->h, sc, err);
+    if (st != PTGPU_OK) return fail(st, err);
+    if (sc.walllight) add_wall_light(sc);      // main(): if (walllight) AddWallLight()
+    if (walllight) *walllight = sc.walllight ? 1 : 0;
+    st = ptgpu_set_shapes(c, sc.shapes.data(), (uint32_t)sc.shapes.size(), sc.light_cnt);
+    if (st != PTGPU_OK) return st;
+    return ptgpu_set_camera(c, &sc.camera);
+}
+
+int ptgpu_set_camera(ptgpu_ctx *c, const ptgpu_camera *cam) {
+    if (!c || !cam) return fail(PTGPU_E_INVAL, "null argument");
+    c->cam = *cam;
+    c->cam.width = (float)c->w;
+    c->cam.height = (float)c->h;
+    update_camera(&c->cam);
+    c->cam_set = true;
+    c->current_sample = 0;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_camera(ptgpu_ctx *c, ptgpu_camera *cam) {
+    if (!c || !cam) return fail(PTGPU_E_INVAL, "null argument");
+    *cam = c->cam;
+    return PTGPU_OK;
+}
+
+static int ensure_bvh_buffers(ptgpu_ctx *c) {
+    const size_t n = c->n;
+    CK(c->d_btn.ensure((n > 1 ? n - 1 : 1) * sizeof(ptgpu_bvh_node)));
+    CK(c->d_btl.ensure(n * sizeof(ptgpu_bvh_node)));
+    CK(c->d_keys.ensure(n * 4));
+    CK(c->d_keys_alt.ensure(n * 4));
+    CK(c->d_keys_tmp.ensure(n * 4));
+    CK(c->d_vals_alt.ensure(n * 4));
+    CK(c->d_vals_tmp.ensure(n * 4));
+    CK(c->d_sorted.ensure(n * 4));
+    CK(c->d_status.ensure(sort_status_words((int)n) * 4));
+    CK(c->d_state.ensure(sizeof(BuildState)));
+    CK(c->d_tile_bounds.ensure(((n + 1023) / 1024) * 6 * sizeof(float)));
+    return PTGPU_OK;
+}
+
+static int prepare_bvh_trace(ptgpu_ctx *c) {
+    const size_t n = c->n;
+    CK(c->d_nodes.ensure((n > 1 ? n - 1 : 1) * 4 * sizeof(float4)));
+    CK(c->d_prims.ensure(n * 3 * sizeof(float4)));
+    CK(c->d_prim_id.ensure(n * 4));
+    CK(c->d_root_box.ensure(6 * sizeof(float)));
+    CK(launch_abi_to_trace(c->d_btn.as<ptgpu_bvh_node>(), c->d_btl.as<ptgpu_bvh_node>(), (int)n,
+                           c->d_prims0.as<float4>(), c->d_nodes.as<float4>(), c->d_prims.as<float4>(),
+                           c->d_prim_id.as<int32_t>(), c->stream));
+    const ptgpu_bvh_node *root = n > 1 ? c->d_btn.as<ptgpu_bvh_node>() : c->d_btl.as<ptgpu_bvh_node>();
+    CK(cudaMemcpyAsync(c->d_root_box.p, &root->bound, 6 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    c->root_first = 0;
+    c->root_count = n > 1 ? 0 : 1;
+    return PTGPU_OK;
+}
+
+int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    if (c->n == 0) return fail(PTGPU_E_STATE, "no shapes set");
+    if (accel < 0 || accel > 2) return fail(PTGPU_E_INVAL, "accel must be 0, 1 or 2");
+    if (flags & (PTGPU_FLAG_MORTON_DELTA | PTGPU_FLAG_TREELET))
+        return fail(PTGPU_E_INVAL, "build flag not supported by this build");
+    cudaSetDevice(c->device);
+    c->accel_built = -1;
+    c->current_sample = 0;
+    if (accel == PTGPU_ACCEL_NONE) {
+        c->accel_built = PTGPU_ACCEL_NONE;
+        c->last_build_ms = 0.f;
+        return PTGPU_OK;
+    }
+    if (accel == PTGPU_ACCEL_BVH) {
+        int st = ensure_bvh_buffers(c);
+        if (st) return st;
+        LbvhBuffers b;
+        b.verts = c->d_verts.as<float>();
+        b.type = c->d_type.as<uint8_t>();
+        b.keys = c->d_keys.as<uint32_t>();
+        b.keys_alt = c->d_keys_alt.as<uint32_t>();
+        b.keys_tmp = c->d_keys_tmp.as<uint32_t>();
+        b.vals_alt = c->d_vals_alt.as<int32_t>();
+        b.vals_tmp = c->d_vals_tmp.as<int32_t>();
+        b.sorted = c->d_sorted.as<int32_t>();
+        b.status = c->d_status.as<uint32_t>();
+        b.state = c->d_state.as<BuildState>();
+        b.tile_bounds = c->d_tile_bounds.as<float>();
+        b.btn = c->d_btn.as<ptgpu_bvh_node>();
+        b.btl = c->d_btl.as<ptgpu_bvh_node>();
+        CK(cudaEventRecord(c->ev0, c->stream));
+        CK(launch_lbvh_build(b, (int)c->n, c->all_tri ? 1 : 0, c->sm_count, c->stream));
+        CK(cudaEventRecord(c->ev1, c->stream));
+        BuildState hs;
+        CK(cudaMemcpyAsync(&hs, c->d_state.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        cudaEventElapsedTime(&c->last_build_ms, c->ev0, c->ev1);
+        if (hs.error) return fail(PTGPU_E_TIMEOUT, "radix sort look-back wait gave up");
+        c->bvh_valid = true;
+        c->shapes_exported = false;
+        st = prepare_bvh_trace(c);
+        if (st) return st;
+        CK(cudaStreamSynchronize(c->stream));
+        c->accel_built = PTGPU_ACCEL_BVH;
+        return PTGPU_OK;
+    }
+    // KD tree: host build with the reference topology, device traversal
+    auto t0 = std::chrono::steady_clock::now();
+    int st = kd_build(c->h_shapes.data(), c->n, c->kd);
+    if (st) return fail(st, "kd build failed");
+    for (uint32_t i = 0; i < c->n; ++i) { c->h_shapes[i].index = (int32_t)i; c->h_shapes[i].morton_code = 0; }
+    std::vector<float> nodes;
+    float root_box[6];
+    kd_trace_nodes(c->kd, nodes, &c->root_first, &c->root_count, root_box);
+    const size_t nk = c->kd.kn.size();
+    CK(c->d_nodes.ensure(nodes.size() * sizeof(float) + 64));
+    CK(c->d_prims.ensure((nk ? nk : 1) * 3 * sizeof(float4)));
+    CK(c->d_prim_id.ensure((nk ? nk : 1) * 4));
+    CK(c->d_root_box.ensure(6 * sizeof(float)));
+    if (!nodes.empty())
+        CK(cudaMemcpyAsync(c->d_nodes.p, nodes.data(), nodes.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    if (nk)
+        CK(cudaMemcpyAsync(c->d_prim_id.p, c->kd.kn.data(), nk * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_root_box.p, root_box, sizeof(root_box), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_gather_prims(c->d_prim_id.as<int32_t>(), (int)nk, c->d_prims0.as<float4>(),
+                           c->d_prims.as<float4>(), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->last_build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    c->kd_valid = true;
+    c->accel_built = PTGPU_ACCEL_KDTREE;
+    return PTGPU_OK;
+}
+
+int ptgpu_last_build_ms(ptgpu_ctx *c, float *ms) {
+    if (!c || !ms) return fail(PTGPU_E_INVAL, "null argument");
+    *ms = c->last_build_ms;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_bvh(ptgpu_ctx *c, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl) {
+    if (!c || !btl || (!btn && c->n > 1)) return fail(PTGPU_E_INVAL, "null argument");
+    if (!c->bvh_valid) return fail(PTGPU_E_STATE, "no BVH has been built");
+    cudaSetDevice(c->device);
+    if (c->n > 1)
+        CK(cudaMemcpyAsync(btn, c->d_btn.p, (size_t)(c->n - 1) * sizeof(ptgpu_bvh_node), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(btl, c->d_btl.p, (size_t)c->n * sizeof(ptgpu_bvh_node), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PTGPU_OK;
+}
+
+int ptgpu_set_bvh(ptgpu_ctx *c, const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, uint32_t n) {
+    if (!c || !btl || (!btn && n > 1)) return fail(PTGPU_E_INVAL, "null argument");
+    if (n != c->n) return fail(PTGPU_E_INVAL, "node count does not match the shape count");
+    for (uint32_t k = 0; k < n; ++k)
+        if (btl[k].nShape < 0 || (uint32_t)btl[k].nShape >= n) return fail(PTGPU_E_INVAL, "leaf shape out of range");
+    for (uint32_t i = 0; i + 1 < n; ++i) {
+        const ptgpu_bvh_node &d = btn[i];
+        bool ll = d.nLeft == d.min, rl = d.nRight == d.max;
+        if (d.nLeft < 0 || d.nRight < 0 || (uint32_t)d.nLeft >= (ll ? n : n - 1) ||
+            (uint32_t)d.nRight >= (rl ? n : n - 1))
+            return fail(PTGPU_E_INVAL, "child index out of range at node " + std::to_string(i));
+    }
+    cudaSetDevice(c->device);
+    int st = ensure_bvh_buffers(c);
+    if (st) return st;
+    if (n > 1) CK(cudaMemcpyAsync(c->d_btn.p, btn, (size_t)(n - 1) * sizeof(ptgpu_bvh_node), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_btl.p, btl, (size_t)n * sizeof(ptgpu_bvh_node), cudaMemcpyHostToDevice, c->stream));
+    c->bvh_valid = true;
+    c->shapes_exported = true;   // shapes keep what the caller set
+    st = prepare_bvh_trace(c);
+    if (st) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    c->accel_built = PTGPU_ACCEL_BVH;
+    c->current_sample = 0;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_kdtree(ptgpu_ctx *c, ptgpu_kd_node *kng, int32_t *kng_cnt, int32_t *kn, int32_t *kn_cnt) {
+    if (!c || !kng_cnt || !kn_cnt) return fail(PTGPU_E_INVAL, "null argument");
+    if (!c->kd_valid) return fail(PTGPU_E_STATE, "no KD tree has been built");
+    int64_t size;
+    int st = kd_heap_size(c->kd, &size);
+    *kn_cnt = c->kd.szbuf;
+    if (size < 0 || size > INT32_MAX) { *kng_cnt = -1; return fail(PTGPU_E_RANGE, "KD heap too large"); }
+    if (!kng || !kn) {          // size query
+        *kng_cnt = (int32_t)size;
+        return st == PTGPU_OK ? PTGPU_OK : fail(st, "KD tree does not fit the int16 layout");
+    }
+    if (*kng_cnt < size) return fail(PTGPU_E_INVAL, "kng buffer too small");
+    *kng_cnt = (int32_t)size;
+    st = kd_export_heap(c->kd, kng, size, kn);
+    if (st) return fail(st, "KD tree does not fit the int16 layout");
+    return PTGPU_OK;
+}
+
+int ptgpu_set_seeds(ptgpu_ctx *c, const uint32_t *seeds) {
+    if (!c || !seeds) return fail(PTGPU_E_INVAL, "null argument");
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(c->d_seeds.p, seeds, (size_t)c->w * c->h * 2 * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PTGPU_OK;
+}
+
+int ptgpu_get_seeds(ptgpu_ctx *c, uint32_t *seeds) {
+    if (!c || !seeds) return fail(PTGPU_E_INVAL, "null argument");
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(seeds, c->d_seeds.p, (size_t)c->w * c->h * 2 * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PTGPU_OK;
+}
+
+int ptgpu_reset_accumulation(ptgpu_ctx *c) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    c->current_sample = 0;
+    return PTGPU_OK;
+}
+
+int ptgpu_get_current_sample(ptgpu_ctx *c, int32_t *cs) {
+    if (!c || !cs) return fail(PTGPU_E_INVAL, "null argument");
+    *cs = c->current_sample;
+    return PTGPU_OK;
+}
+
+static int enqueue_render(ptgpu_ctx *c, uint32_t passes) {
+    if (c->accel_built < 0) return fail(PTGPU_E_STATE, "build an acceleration structure first");
+    if (!c->cam_set) return fail(PTGPU_E_STATE, "set a camera first");
+    if (passes == 0) return PTGPU_OK;
+    RenderArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.tv = make_view(c);
+    a.mats = c->d_mats.as<Material>();
+    a.prims0 = c->d_prims0.as<float4>();
+    a.lights = c->d_lights.as<LightRec>();
+    a.n_lights = c->n_lights;
+    a.cam = c->cam;
+    a.width = c->w;
+    a.height = c->h;
+    a.start_sample = c->current_sample;
+    a.passes = (int32_t)passes;
+    a.max_depth = c->max_depth;
+    a.rtl = c->rtl;
+    a.colors = c->d_colors.as<ptgpu_vec>();
+    a.pixels = c->d_pixels.as<uint32_t>();
+    a.seeds = c->d_seeds.as<uint32_t>();
+    CK(launch_render(a, c->block, c->stream));
+    c->current_sample += (int)passes;
+    return PTGPU_OK;
+}
+
+static int check_err_flags(ptgpu_ctx *c) {
+    int32_t flags = 0;
+    CK(cudaMemcpyAsync(&flags, c->d_err.p, 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (flags & 1) {
+        cudaMemsetAsync(c->d_err.p, 0, 4, c->stream);
+        return fail(PTGPU_E_RANGE, "traversal stack overflow (tree deeper than 64 levels)");
+    }
+    return PTGPU_OK;
+}
+
+int ptgpu_draw_frame(ptgpu_ctx *c, uint32_t passes, const uint32_t **pixels_out) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    cudaSetDevice(c->device);
+    int st = enqueue_render(c, passes);
+    if (st) return st;
+    CK(cudaMemcpyAsync(c->h_pixels, c->d_pixels.p, (size_t)c->w * c->h * 4, cudaMemcpyDeviceToHost, c->stream));
+    st = check_err_flags(c);
+    if (st) return st;
+    if (pixels_out) *pixels_out = c->h_pixels;
+    return PTGPU_OK;
+}
+
+int ptgpu_render_async(ptgpu_ctx *c, uint32_t passes) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    cudaSetDevice(c->device);
+    return enqueue_render(c, passes);
+}
+
+int ptgpu_synchronize(ptgpu_ctx *c) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    cudaSetDevice(c->device);
+    CK(cudaStreamSynchronize(c->stream));
+    return check_err_flags(c);
+}
+
+int ptgpu_get_colors(ptgpu_ctx *c, ptgpu_vec *colors) {
+    if (!c || !colors) return fail(PTGPU_E_INVAL, "null argument");
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(colors, c->d_colors.p, (size_t)c->w * c->h * sizeof(ptgpu_vec), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PTGPU_OK;
+}
+
+int ptgpu_get_pixels(ptgpu_ctx *c, uint32_t *pixels) {
+    if (!c || !pixels) return fail(PTGPU_E_INVAL, "null argument");
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(pixels, c->d_pixels.p, (size_t)c->w * c->h * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PTGPU_OK;
+}
+
+int ptgpu_trace_closest_device(ptgpu_ctx *c, const ptgpu_ray *d_rays, uint32_t n, float *d_t,
+                               uint32_t *d_id, int32_t *d_hit) {
+    if (!c || (n && (!d_rays || !d_t || !d_id || !d_hit))) return fail(PTGPU_E_INVAL, "null argument");
+    if (c->accel_built < 0) return fail(PTGPU_E_STATE, "build an acceleration structure first");
+    cudaSetDevice(c->device);
+    CK(launch_trace_closest(make_view(c), d_rays, (int)n, d_t, d_id, d_hit, c->stream));
+    return PTGPU_OK;
+}
+
+int ptgpu_trace_closest(ptgpu_ctx *c, const ptgpu_ray *rays, uint32_t n, float *t, uint32_t *id,
+                        int32_t *hit) {
+    if (!c || (n && (!rays || !t || !id || !hit))) return fail(PTGPU_E_INVAL, "null argument");
+    if (c->accel_built < 0) return fail(PTGPU_E_STATE, "build an acceleration structure first");
+    if (n == 0) return PTGPU_OK;
+    cudaSetDevice(c->device);
+    CK(c->d_rays.ensure((size_t)n * sizeof(ptgpu_ray)));
+    CK(c->d_t.ensure((size_t)n * 4));
+    CK(c->d_id.ensure((size_t)n * 4));
+    CK(c->d_hit.ensure((size_t)n * 4));
+    CK(cudaMemcpyAsync(c->d_rays.p, rays, (size_t)n * sizeof(ptgpu_ray), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_trace_closest(make_view(c), c->d_rays.as<ptgpu_ray>(), (int)n, c->d_t.as<float>(),
+                            c->d_id.as<uint32_t>(), c->d_hit.as<int32_t>(), c->stream));
+    CK(cudaMemcpyAsync(t, c->d_t.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(id, c->d_id.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hit, c->d_hit.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    return check_err_flags(c);
+}
+
+}  // extern "C"

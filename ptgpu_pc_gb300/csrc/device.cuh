@@ -1,0 +1,267 @@
+// device.cuh -- device-side math and data layouts shared by the kernels.
+//
+// Float semantics: the library is compiled with -fmad=false and IEEE
+// division/square root, so every expression below rounds exactly like the
+// reference's OpenCL C (rendering_kernel.cl) evaluated without contraction.
+// The helpers are written operand-for-operand in the reference's order.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/ptgpu.h"
+#include "types.h"
+
+namespace ptgpu {
+
+constexpr float kEps = 0.01f;                       // EPSILON, geom.h:29
+constexpr float kPi = 3.14159265358979323846f;      // FLOAT_PI, geom.h:30
+constexpr float kInfT = 1e20f;                      // Intersect's initial t
+constexpr int kStackSize = 64;                      // traversal stack entries
+
+struct f3 { float x, y, z; };
+
+__host__ __device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 v; v.x = x; v.y = y; v.z = z; return v; }
+__host__ __device__ __forceinline__ f3 sub3(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ f3 add3(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ f3 mul3(f3 a, f3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__host__ __device__ __forceinline__ f3 smul3(float k, f3 b) { return mk3(k * b.x, k * b.y, k * b.z); }
+__host__ __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// vnorm (vec.h:41): 1.f / sqrt(dot) then scale
+__device__ __forceinline__ f3 norm3(f3 v) { float l = 1.f / sqrtf(dot3(v, v)); return smul3(l, v); }
+__host__ __device__ __forceinline__ bool iszero3(f3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
+// OpenCL sign(): +-1, the signed zero itself, 0 for NaN
+__device__ __forceinline__ float cl_sign(float x) {
+    return x > 0.f ? 1.f : (x < 0.f ? -1.f : (x == x ? x : 0.f));
+}
+__device__ __forceinline__ float cl_clamp(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+// ternary min/max of AccelCommon.h:14-32 and BVH.cl:78-86 (bounds)
+__host__ __device__ __forceinline__ float min2f(float a, float b) { return (a < b) ? a : b; }
+__host__ __device__ __forceinline__ float max2f(float a, float b) { return (a > b) ? a : b; }
+
+// GetRandom (rendering_kernel.cl:4-17, simplernd.h:35-49)
+__device__ __forceinline__ float get_random(uint32_t &s0, uint32_t &s1) {
+    s0 = 36969u * (s0 & 65535u) + (s0 >> 16);
+    s1 = 18000u * (s1 & 65535u) + (s1 >> 16);
+    uint32_t ires = (s0 << 16) + s1;
+    float f = __uint_as_float((ires & 0x007fffffu) | 0x40000000u);
+    return (f - 2.f) / 2.f;
+}
+
+__device__ __forceinline__ float tri_intersect(f3 p1, f3 e1, f3 e2, f3 o, f3 d) {
+    f3 pvec = cross3(d, e2);
+    float det = dot3(e1, pvec);
+    if (det == 0.f) return 0.f;
+    float inv_det = 1.f / det;
+    f3 tvec = sub3(o, p1);
+    float u = dot3(tvec, pvec) * inv_det;
+    if (u < 0.f || u > 1.f) return 0.f;
+    f3 qvec = cross3(tvec, e1);
+    float v = dot3(d, qvec) * inv_det;
+    if (v < 0.f || u + v > 1.f) return 0.f;
+    float t = dot3(e2, qvec) * inv_det;
+    return t > kEps ? t : 0.f;
+}
+
+__device__ __forceinline__ float sphere_intersect(f3 p, float rad2, f3 o, f3 d) {
+    f3 op = sub3(p, o);
+    float b = dot3(op, d);
+    float det = b * b - dot3(op, op) + rad2;
+    if (det < 0.f) return 0.f;
+    det = sqrtf(det);
+    float t = b - det;
+    if (t > kEps) return t;
+    t = b + det;
+    if (t > kEps) return t;
+    return 0.f;
+}
+
+__device__ __forceinline__ float prim_intersect(const float4 *prims, int k, f3 o, f3 d) {
+    float4 a = __ldg(&prims[3 * k + 0]);
+    float4 b = __ldg(&prims[3 * k + 1]);
+    if (__float_as_int(a.w) == PTGPU_TRIANGLE) {
+        float4 c = __ldg(&prims[3 * k + 2]);
+        return tri_intersect(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), o, d);
+    }
+    return sphere_intersect(mk3(a.x, a.y, a.z), b.x, o, d);
+}
+
+// intersection_bound_test (rendering_kernel.cl:140-192) on one box, with the
+// reciprocal direction precomputed (1.0/d rounded to float == 1.f/d).
+__device__ __forceinline__ bool slab(float bminx, float bmaxx, float bminy, float bmaxy,
+                                     float bminz, float bmaxz, f3 o, f3 inv, float &tmin,
+                                     float &tmax) {
+    float txmin, txmax, tymin, tymax, tzmin, tzmax;
+    if (inv.x >= 0) { txmin = (bminx - o.x) * inv.x; txmax = (bmaxx - o.x) * inv.x; }
+    else            { txmin = (bmaxx - o.x) * inv.x; txmax = (bminx - o.x) * inv.x; }
+    if (inv.y >= 0) { tymin = (bminy - o.y) * inv.y; tymax = (bmaxy - o.y) * inv.y; }
+    else            { tymin = (bmaxy - o.y) * inv.y; tymax = (bminy - o.y) * inv.y; }
+    if (inv.z >= 0) { tzmin = (bminz - o.z) * inv.z; tzmax = (bmaxz - o.z) * inv.z; }
+    else            { tzmin = (bmaxz - o.z) * inv.z; tzmax = (bminz - o.z) * inv.z; }
+    tmin = fmaxf(txmin, fmaxf(tymin, tzmin));
+    tmax = fminf(txmax, fminf(tymax, tzmax));
+    return tmin <= tmax;
+}
+
+// A box is entered when the reference's test passes and it can still hold a
+// hit that improves on tbest: entry below tbest (with a 1e-4 relative margin
+// for rounding) and exit in front of the origin.
+__device__ __forceinline__ bool enter_box(bool hit, float tmin, float tmax, float tbest) {
+    return hit && tmin <= tbest * 1.0001f && tmax >= 0.f;
+}
+
+// Closest hit: returns 1 when any prim reported a non-zero distance (the
+// reference's `intersected`), t/id/prim of the nearest.  Front-to-back order.
+__device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, float &t,
+                                             int &prim, int &id) {
+    t = kInfT;
+    prim = -1;
+    id = 0;
+    int hit_any = 0;
+    if (tv.n_shapes <= 0) return 0;
+    if (tv.accel == PTGPU_ACCEL_NONE) {
+        for (int i = tv.n_shapes - 1; i >= 0; --i) {
+            float dd = prim_intersect(tv.prims, i, o, d);
+            if (dd != 0.f && dd < t) { t = dd; prim = i; }
+        }
+        if (prim >= 0) id = prim;
+        return t < kInfT;
+    }
+    f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    float tmin, tmax;
+    bool rh = slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
+                   __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o,
+                   inv, tmin, tmax);
+    if (!rh) return 0;
+    int stack[kStackSize];
+    int sp = 0;
+    int node_ref, node_cnt;
+    if (tv.root_count > 0) { node_ref = tv.root_first; node_cnt = tv.root_count; }
+    else { node_ref = 0; node_cnt = 0; }
+    // stack entries: internal node index (>= 0) or leaf ~(first | count<<26)?
+    // Leaves are tested as soon as their box passes, so only nodes are pushed.
+    for (;;) {
+        if (node_cnt > 0) {
+            for (int k = node_ref; k < node_ref + node_cnt; ++k) {
+                float dd = prim_intersect(tv.prims, k, o, d);
+                if (dd != 0.f) {
+                    hit_any = 1;
+                    if (dd < t) { t = dd; prim = k; }
+                }
+            }
+        } else {
+            const float4 *nd = tv.nodes + 4 * node_ref;
+            float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+            int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+            float lt0, lt1, rt0, rt1;
+            bool lh = slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv, lt0, lt1);
+            bool rhh = slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv, rt0, rt1);
+            lh = enter_box(lh, lt0, lt1, t);
+            rhh = enter_box(rhh, rt0, rt1, t);
+            // leaves are intersected immediately (their box was just tested)
+            if (lh && q3.z > 0) {
+                for (int k = q3.x; k < q3.x + q3.z; ++k) {
+                    float dd = prim_intersect(tv.prims, k, o, d);
+                    if (dd != 0.f) { hit_any = 1; if (dd < t) { t = dd; prim = k; } }
+                }
+                lh = false;
+            }
+            if (rhh && q3.w > 0) {
+                for (int k = q3.y; k < q3.y + q3.w; ++k) {
+                    float dd = prim_intersect(tv.prims, k, o, d);
+                    if (dd != 0.f) { hit_any = 1; if (dd < t) { t = dd; prim = k; } }
+                }
+                rhh = false;
+            }
+            if (lh && rhh) {
+                int nearc = q3.x, farc = q3.y;
+                if (rt0 < lt0) { nearc = q3.y; farc = q3.x; }
+                if (sp < kStackSize) stack[sp++] = farc;
+                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+                node_ref = nearc; node_cnt = 0;
+                continue;
+            }
+            if (lh) { node_ref = q3.x; node_cnt = 0; continue; }
+            if (rhh) { node_ref = q3.y; node_cnt = 0; continue; }
+        }
+        if (sp == 0) break;
+        node_ref = stack[--sp];
+        node_cnt = 0;
+    }
+    if (prim >= 0) id = __ldg(&tv.prim_id[prim]);
+    return hit_any;
+}
+
+// IntersectP (rendering_kernel.cl:375-395): any hit with 0 < d < maxt among
+// shapes 0..n-2 (the last shape is never tested), accelerated.
+__device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float maxt) {
+    const int skip = tv.n_shapes - 1;
+    if (tv.n_shapes <= 1) return false;
+    if (tv.accel == PTGPU_ACCEL_NONE) {
+        for (int i = tv.n_shapes - 2; i >= 0; --i) {
+            float dd = prim_intersect(tv.prims, i, o, d);
+            if (dd != 0.f && dd < maxt) return true;
+        }
+        return false;
+    }
+    f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    float tmin, tmax;
+    if (!slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
+              __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, inv,
+              tmin, tmax))
+        return false;
+    int stack[kStackSize];
+    int sp = 0;
+    int node_ref = tv.root_count > 0 ? tv.root_first : 0;
+    int node_cnt = tv.root_count > 0 ? tv.root_count : 0;
+    for (;;) {
+        if (node_cnt > 0) {
+            for (int k = node_ref; k < node_ref + node_cnt; ++k) {
+                if (__ldg(&tv.prim_id[k]) == skip) continue;
+                float dd = prim_intersect(tv.prims, k, o, d);
+                if (dd != 0.f && dd < maxt) return true;
+            }
+        } else {
+            const float4 *nd = tv.nodes + 4 * node_ref;
+            float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+            int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+            float lt0, lt1, rt0, rt1;
+            bool lh = enter_box(slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv, lt0, lt1), lt0, lt1, maxt);
+            bool rhh = enter_box(slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv, rt0, rt1), rt0, rt1, maxt);
+            if (lh && q3.z > 0) {
+                for (int k = q3.x; k < q3.x + q3.z; ++k) {
+                    if (__ldg(&tv.prim_id[k]) == skip) continue;
+                    float dd = prim_intersect(tv.prims, k, o, d);
+                    if (dd != 0.f && dd < maxt) return true;
+                }
+                lh = false;
+            }
+            if (rhh && q3.w > 0) {
+                for (int k = q3.y; k < q3.y + q3.w; ++k) {
+                    if (__ldg(&tv.prim_id[k]) == skip) continue;
+                    float dd = prim_intersect(tv.prims, k, o, d);
+                    if (dd != 0.f && dd < maxt) return true;
+                }
+                rhh = false;
+            }
+            if (lh && rhh) {
+                int nearc = q3.x, farc = q3.y;
+                if (rt0 < lt0) { nearc = q3.y; farc = q3.x; }
+                if (sp < kStackSize) stack[sp++] = farc;
+                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+                node_ref = nearc; node_cnt = 0;
+                continue;
+            }
+            if (lh) { node_ref = q3.x; node_cnt = 0; continue; }
+            if (rhh) { node_ref = q3.y; node_cnt = 0; continue; }
+        }
+        if (sp == 0) break;
+        node_ref = stack[--sp];
+        node_cnt = 0;
+    }
+    return false;
+}
+
+}  // namespace ptgpu

@@ -1,0 +1,70 @@
+// lbvh.h -- host-side interface of the GPU LBVH build and of the traversal
+// data preparation (lbvh.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/ptgpu.h"
+#include "types.h"
+
+namespace ptgpu {
+
+// Per-build device state, zeroed by the first kernel of every build.
+struct BuildState {
+    uint32_t hist[4][256];      // digit histograms of the four radix passes
+    uint32_t tile_counter[4];   // dynamic tile ids of the onesweep passes
+    uint32_t cmin[3], cmax[3];  // centroid bounds as order-preserving uints
+    uint32_t error;             // bit 0: a look-back wait gave up
+    uint32_t top_ticket;
+};
+
+struct LbvhBuffers {
+    const float *verts;         // 9 floats per shape (p1,p2,p3 or centre,rad)
+    const uint8_t *type;        // PTGPU_SPHERE / PTGPU_TRIANGLE per shape
+    uint32_t *keys;             // ~Morton code per shape (sort key)
+    uint32_t *keys_alt, *keys_tmp;
+    int32_t *vals_alt, *vals_tmp;
+    int32_t *sorted;            // sorted_geometry_indices
+    uint32_t *status;           // look-back words, sort_status_words(n)
+    BuildState *state;
+    float *tile_bounds;         // 6 floats per 1024-leaf tile
+    ptgpu_bvh_node *btn, *btl;  // the reference's output arrays
+};
+
+size_t sort_status_words(int n);
+
+cudaError_t launch_unpack_shapes(const ptgpu_shape *d_shapes, int n, float *verts, uint8_t *type,
+                                 float4 *prims, Material *mats, cudaStream_t s);
+cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_count,
+                              cudaStream_t s);
+cudaError_t launch_abi_to_trace(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, int n,
+                                const float4 *prims0, float4 *nodes, float4 *prims,
+                                int32_t *prim_id, cudaStream_t s);
+cudaError_t launch_gather_prims(const int32_t *order, int count, const float4 *prims0,
+                                float4 *prims, cudaStream_t s);
+cudaError_t launch_export_shapes(ptgpu_shape *shapes, const float *verts, const uint8_t *type,
+                                 const uint32_t *keys, int n, cudaStream_t s);
+
+// trace.cu
+struct RenderArgs {
+    TraceView tv;
+    const Material *mats;
+    const float4 *prims0;       // shape-order prims (geometry of shape 0 for a
+                                // hit reported beyond t = 1e20)
+    const LightRec *lights;
+    int32_t n_lights;
+    ptgpu_camera cam;
+    int32_t width, height;
+    int32_t start_sample, passes;
+    int32_t max_depth;
+    int32_t rtl;                // evaluate light-sample random pairs right-to-left
+    ptgpu_vec *colors;          // W*H, row-flipped (RadianceGPU)
+    uint32_t *pixels;           // W*H RGBA8
+    uint32_t *seeds;            // 2*W*H
+};
+cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
+cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
+                                 uint32_t *id, int32_t *hit, cudaStream_t s);
+
+}  // namespace ptgpu

@@ -1,0 +1,91 @@
+"""GPU LBVH build vs the oracle (CLBVH + BVH.cl restated): Morton keys, the
+sorted permutation, and the btn/btl arrays byte for byte."""
+import numpy as np
+import pytest
+
+from ptgpu_pc_gb300 import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_build(shapes, light_cnt=0):
+    import ptgpu_pc_gb300 as pt
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, light_cnt)
+        ctx.build(abi.ACCEL_BVH)
+        btn, btl = ctx.get_bvh()
+        out = ctx.get_shapes()
+        ms = ctx.last_build_ms()
+    return out, btn, btl, ms
+
+
+def _compare(shapes, orc):
+    g_shapes, g_btn, g_btl, _ = _gpu_build(shapes)
+    o_shapes, o_btn, o_btl, o_sorted = orc.build_bvh(shapes)
+    assert (g_shapes["morton_code"] == o_shapes["morton_code"]).all()
+    assert (g_shapes["index"] == o_shapes["index"]).all()
+    assert g_shapes["b"].tobytes() == o_shapes["b"].tobytes()
+    assert (g_btl["nShape"] == o_sorted).all()
+    assert g_btl.tobytes() == o_btl.tobytes()
+    assert g_btn.tobytes() == o_btn.tobytes()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 13, 100, 1000, 1023, 1024, 1025, 2047, 4097, 12345])
+def test_lbvh_soup_small(n, built_lib, orc):
+    _compare(scenes.triangle_soup(n, seed=n), orc)
+
+
+def test_lbvh_cornell_spheres(built_lib, orc):
+    _compare(scenes.cornell_spheres()[0], orc)
+
+
+def test_lbvh_icosphere_scene(built_lib, orc):
+    _compare(scenes.icosphere_scene(level=6)[0], orc)
+
+
+def test_lbvh_duplicate_keys_and_flat_axis(built_lib, orc):
+    # every centroid in the z = 0 plane (flat axis: max == min -> code bits 0)
+    # and many identical triangles (duplicate keys: the sort must stay stable)
+    s = scenes.triangle_soup(5000, seed=11)
+    for f in ("p1", "p2", "p3"):
+        s[f][:, 2] = 0.0
+    s[1000:3000] = s[1000]
+    _compare(s, orc)
+
+
+def test_lbvh_negative_coordinates(built_lib, orc):
+    # all centroids negative: the reference's FLT_MIN initial maximum is kept
+    s = scenes.triangle_soup(3000, seed=12)
+    for f in ("p1", "p2", "p3"):
+        s[f] -= 10.0
+    _compare(s, orc)
+
+
+@pytest.mark.parametrize("n", [1 << 20, (1 << 20) + 7])
+def test_lbvh_1m(n, built_lib, orc):
+    _compare(scenes.triangle_soup(n, seed=5), orc)
+
+
+def test_lbvh_4m_properties(built_lib):
+    """4M triangles: size-independent checks -- each shape exactly once in the
+    leaves, keys non-increasing along the leaves, every internal bound equal
+    to the union of its children, parents consistent."""
+    n = 1 << 22
+    shapes = scenes.triangle_soup(n, seed=6)
+    g_shapes, btn, btl, ms = _gpu_build(shapes)
+    order = btl["nShape"]
+    assert np.array_equal(np.sort(order), np.arange(n))
+    keys = g_shapes["morton_code"][order]
+    assert (keys[:-1] >= keys[1:]).all()
+    # stability: equal keys keep index order
+    eq = keys[:-1] == keys[1:]
+    assert (order[:-1][eq] < order[1:][eq]).all()
+    ll = btn["nLeft"] == btn["min"]
+    rl = btn["nRight"] == btn["max"]
+    lb = np.where(ll[:, None], btl["bound"][btn["nLeft"]], btn["bound"][np.minimum(btn["nLeft"], n - 2)])
+    rb = np.where(rl[:, None], btl["bound"][btn["nRight"]], btn["bound"][np.minimum(btn["nRight"], n - 2)])
+    mins = np.where(lb[:, 0::2] < rb[:, 0::2], lb[:, 0::2], rb[:, 0::2])
+    maxs = np.where(lb[:, 1::2] > rb[:, 1::2], lb[:, 1::2], rb[:, 1::2])
+    assert np.array_equal(btn["bound"][:, 0::2], mins)
+    assert np.array_equal(btn["bound"][:, 1::2], maxs)
+    assert ms > 0
