@@ -401,6 +401,7 @@ __device__ __forceinline__ void emit_internal(ptgpu_bvh_node *btn, int lo, int h
     int32_t a_lo, a_hi, a_g;
     topo_range(lo, n, a_lo, a_hi, a_g);
     int idx = (a_lo == lo && a_hi == hi) ? lo : hi;
+    if (idx < 0 || idx > n - 2) return;   // unreachable for a valid block; keeps writes in bounds
     int gamma = lo + (1 << (level - 1)) - 1;
     bool ll = (level == 1), rl = (hi == gamma + 1);
     int parent = topo_parent_internal(idx, lo, hi, n);
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float *__restrict_
     const int cnt = min(kTileLeaves, n - T0);
     for (int k = threadIdx.x; k < cnt; k += kTileThreads) {
         int leaf = T0 + k;
-        int s = sorted[leaf];
+        int s = min(max(sorted[leaf], 0), n - 1);   // in bounds even after a failed sort
         bool tri = all_tri || type[s] == PTGPU_TRIANGLE;
         float b[6];
         shape_bound(verts, s, tri, b);
@@ -495,7 +496,7 @@ __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
                                float4 *__restrict__ prims, int32_t *__restrict__ prim_id) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        int s = btl[i].nShape;
+        int s = min(max(btl[i].nShape, 0), n - 1);
         prim_id[i] = s;
         prims[3 * (size_t)i + 0] = prims0[3 * (size_t)s + 0];
         prims[3 * (size_t)i + 1] = prims0[3 * (size_t)s + 1];
@@ -504,13 +505,15 @@ __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
     if (i < n - 1) {
         const ptgpu_bvh_node nd = btn[i];
         bool ll = nd.nLeft == nd.min, rl = nd.nRight == nd.max;
-        const ptgpu_bound lb = ll ? btl[nd.nLeft].bound : btn[nd.nLeft].bound;
-        const ptgpu_bound rb = rl ? btl[nd.nRight].bound : btn[nd.nRight].bound;
+        const int li = min(max(nd.nLeft, 0), ll ? n - 1 : n - 2);
+        const int ri = min(max(nd.nRight, 0), rl ? n - 1 : n - 2);
+        const ptgpu_bound lb = ll ? btl[li].bound : btn[li].bound;
+        const ptgpu_bound rb = rl ? btl[ri].bound : btn[ri].bound;
         float4 *o = nodes + 4 * (size_t)i;
         o[0] = make_float4(lb.min_x, lb.max_x, lb.min_y, lb.max_y);
         o[1] = make_float4(lb.min_z, lb.max_z, rb.min_x, rb.max_x);
         o[2] = make_float4(rb.min_y, rb.max_y, rb.min_z, rb.max_z);
-        int4 q = make_int4(nd.nLeft, nd.nRight, ll ? 1 : 0, rl ? 1 : 0);
+        int4 q = make_int4(li, ri, ll ? 1 : 0, rl ? 1 : 0);
         o[3] = *reinterpret_cast<float4 *>(&q);
     }
 }
