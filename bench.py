@@ -1,0 +1,380 @@
+"""Benchmark: the plain path tracer on the displaced-icosphere scene.
+
+One step = one 512x512 frame of 16 passes (samples per pixel) at max depth 8
+through the BVH, scene and tree resident in HBM, L2 flushed between steps.
+value = Msamples/s over all ranks (each rank renders its own replica: the
+path shards by scene/pixels with no data exchange, so N>1 is weak scaling).
+
+Extra keys on the JSON line:
+  e2e          the same metric through the C ABI with host buffers: per step
+               set_shapes (H2D), BVH build, set_seeds (H2D), draw_frame
+               (16 passes, D2H pixels), wall clock
+  roofline     the render kernel against HBM, bytes per query after the
+               closest-hit model (24 B ray + 8 B hit + 60 B per node visit +
+               36 B per primitive test), counts measured by the GPU
+  lbvh         LBVH build of 4,194,304 random triangles: Mtris/s and its HBM
+               roofline at 252 algorithmic bytes per triangle
+  closest_hit  2^24 random rays against the 4M-triangle BVH: Mrays/s
+  cpu_baseline the oracle port (C, OpenMP, all host threads) on a bounded
+               sample of the same frame
+--impl reference times that CPU path alone (rank 0) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = H = 512
+SPP = 16
+MAX_DEPTH = 8
+LBVH_N = 1 << 22
+RAYS_N = 1 << 24
+L2_FLUSH_BYTES = 256 << 20
+WORKLOAD = "icosphere_81934tri_512x512_16spp_depth8_bvh"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, nm in enumerate(names):
+                if s[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def reduce_max(value, pg, device):
+    """max over ranks (a float); identity without a process group."""
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+class CpuReference:
+    """The oracle port (the reference algorithm restated in C, OpenMP over
+    rows) on a bounded block of pixels at the centre of the same frame: the
+    block is sized once so one timed sample runs for about target_s seconds."""
+
+    def __init__(self, shapes, light_cnt, cam, target_s=10.0, threads=0):
+        import oracle
+        from ptgpu_pc_gb300 import abi
+        oracle.build()
+        self.oracle = oracle
+        self.shapes, self.lc = shapes, light_cnt
+        c = np.array(cam, abi.CAMERA)
+        c["width"], c["height"] = W, H
+        self.cam = oracle.update_camera(c)
+        _, btn, btl, _ = oracle.build_bvh(shapes)
+        self.acc = oracle.make_accel(abi.ACCEL_BVH, btn, btl, reference_leafness=True)
+        self.seeds = oracle.make_seeds(1, 2 * W * H)
+        self.threads = threads or os.cpu_count() or 1
+        # calibrate on one row of 16 pixels per thread
+        self.rows, self.cols = 1, 16 * self.threads
+        dt = self._run()
+        px_per_s = self.rows * self.cols / max(dt, 1e-6)
+        want = max(self.threads, int(px_per_s * target_s))
+        self.cols = min(W, want)
+        self.rows = max(1, min(H, want // self.cols))
+
+    def _run(self):
+        r0, c0 = H // 2 - self.rows // 2, W // 2 - self.cols // 2
+        t0 = time.perf_counter()
+        self.oracle.render(self.shapes, self.lc, self.cam, W, H, self.seeds, 1, accel=self.acc,
+                           max_depth=MAX_DEPTH, threads=self.threads, rows=(r0, r0 + self.rows),
+                           cols=(c0, c0 + self.cols))
+        return time.perf_counter() - t0
+
+    def sample(self):
+        dt = self._run()
+        px = self.rows * self.cols
+        desc = ("%dx%d pixel block at the centre of the %dx%d frame, 1 pass, depth %d, BVH built "
+                "by the oracle, brute-force shadow rays as in IntersectP; %.1f s" %
+                (self.cols, self.rows, W, H, MAX_DEPTH, dt))
+        return px / dt / 1e6, self.threads, desc
+
+
+def run_reference(args, rank, world, pg):
+    from ptgpu_pc_gb300 import scenes
+    if rank != 0:
+        return
+    shapes, lc, cam = scenes.icosphere_scene(level=6)
+    per_step = []
+    desc = ""
+    cores = 0
+    per = max(1.0, min(args.ref_seconds, 150.0 / (args.warmup + args.steps)))
+    ref = CpuReference(shapes, lc, cam, target_s=per)
+    for i in range(args.warmup + args.steps):
+        v, cores, desc = ref.sample()
+        if i >= args.warmup:
+            per_step.append(v)
+    value = float(np.mean(per_step))
+    ms_per_step = W * H * SPP / (value * 1e6) * 1e3
+    line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced icosphere)",
+            "config": {"workload": WORKLOAD, "shapes": int(len(shapes)), "width": W, "height": H,
+                       "spp": SPP, "max_depth": MAX_DEPTH, "accel": "bvh"},
+            "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": cores, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def bench_lbvh(pt, abi, scenes, torch, warmup, steps):
+    shapes = scenes.triangle_soup(LBVH_N, seed=3)
+    ctx = pt.Context(8, 8)
+    ctx.set_shapes(shapes, 0)
+    del shapes
+    times = []
+    for i in range(warmup + steps):
+        ctx.build(abi.ACCEL_BVH)
+        if i >= warmup:
+            times.append(ctx.last_build_ms())
+    ms = float(np.mean(times))
+    return ctx, {"metric": "LBVH Mtris/s", "n_tris": LBVH_N, "value": LBVH_N / ms / 1e3,
+                 "unit": "Mtris/s", "ms": ms, "min_ms": float(np.min(times)), "builds": steps}
+
+
+def bench_closest(ctx, torch, scenes, warmup, steps):
+    rays = scenes.random_rays(RAYS_N, seed=4)
+    d_rays = torch.from_numpy(rays.view(np.uint8).reshape(-1)).cuda()
+    del rays
+    d_t = torch.empty(RAYS_N, dtype=torch.float32, device="cuda")
+    d_id = torch.empty(RAYS_N, dtype=torch.int32, device="cuda")
+    d_hit = torch.empty(RAYS_N, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ms = []
+    for i in range(warmup + steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.trace_closest_device(d_rays.data_ptr(), RAYS_N, d_t.data_ptr(), d_id.data_ptr(),
+                                 d_hit.data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        if i >= warmup:
+            ms.append(e0.elapsed_time(e1))
+    hits = int(d_hit.sum().item())
+    m = float(np.mean(ms))
+    return {"metric": "closest-hit Mrays/s", "rays": RAYS_N, "n_tris": LBVH_N,
+            "value": RAYS_N / m / 1e3, "unit": "Mrays/s", "ms": m, "hit_fraction": hits / RAYS_N}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip lbvh/closest-hit/cpu legs")
+    args = ap.parse_args()
+    rank, world, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, pg)
+        return
+
+    import torch
+    import ptgpu_pc_gb300 as pt
+    from ptgpu_pc_gb300 import abi, scenes
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+
+    shapes, lc, cam = scenes.icosphere_scene(level=6)
+    ctx = pt.Context(W, H, accel=abi.ACCEL_BVH, max_depth=MAX_DEPTH, device=local)
+    ctx.set_shapes(shapes, lc)
+    ctx.build(abi.ACCEL_BVH)
+    ctx.set_camera(cam)
+    seeds = pt.make_seeds(1 + rank, 2 * W * H)
+    ctx.set_seeds(seeds)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+
+    # warm-up
+    for _ in range(args.warmup):
+        ctx.reset()
+        ctx.render_async(SPP)
+    ctx.synchronize()
+
+    # timed region: per-step events around the render launch, L2 flushed
+    # between steps outside the events
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    launches = 0
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        ctx.reset()
+        starts[i].record(stream)
+        ctx.render_async(SPP)
+        launches += 1
+        ends[i].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    barrier(pg)
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = sum(step_ms) / 1e3
+    dev_s_max = reduce_max(dev_s, pg, device)
+    samples_all = world * W * H * SPP * args.steps
+    value = samples_all / dev_s_max / 1e6
+
+    # counters for the bytes-moved model (one extra, untimed frame)
+    ctx.reset()
+    st = ctx.render_stats(SPP)
+    ext_v, ext_p, sh_v, sh_p, ext_q, sh_q = (int(x) for x in st)
+    bytes_frame = (24 + 8) * (ext_q + sh_q) + 60 * (ext_v + sh_v) + 36 * (ext_p + sh_p)
+    avg_ms = dev_s / args.steps
+    hbm_peak, peak_kind = peaks()
+    achieved = bytes_frame / (avg_ms / 1e3) / 1e9
+
+    # e2e through the C ABI with host buffers
+    e2e_steps = max(1, args.e2e_steps)
+    ctx_e = pt.Context(W, H, accel=abi.ACCEL_BVH, max_depth=MAX_DEPTH, device=local)
+    ctx_e.set_camera(cam)
+    h2d = shapes.nbytes + seeds.nbytes
+    d2h = W * H * 4
+    ctx_e.set_shapes(shapes, lc); ctx_e.build(abi.ACCEL_BVH); ctx_e.set_seeds(seeds)
+    ctx_e.draw_frame(SPP)                     # warm-up
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx_e.set_shapes(shapes, lc)
+        ctx_e.build(abi.ACCEL_BVH)
+        ctx_e.set_seeds(seeds)
+        pix = ctx_e.draw_frame_view(SPP)
+    e2e_s = reduce_max(time.perf_counter() - t0, pg, device)
+    e2e_value = world * W * H * SPP * e2e_steps / e2e_s / 1e6
+    ctx_e.close()
+
+    line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": avg_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded displaced icosphere, 81,934 shapes)",
+            "config": {"workload": WORKLOAD, "shapes": int(len(shapes)), "width": W, "height": H,
+                       "spp": SPP, "max_depth": MAX_DEPTH, "accel": "bvh", "l2": "flushed between steps (256 MB write)",
+                       "parallelism": "replicas x%d" % world},
+            "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                    "per_step": "set_shapes + BVH build + set_seeds + draw_frame(16)"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "k_render",
+                         "model": "per query 32 B + 60 B/node visit + 36 B/prim test, GPU-counted",
+                         "bytes_per_frame": bytes_frame,
+                         "counts": {"ext_queries": ext_q, "shadow_queries": sh_q,
+                                    "ext_node_visits": ext_v, "ext_prim_tests": ext_p,
+                                    "shadow_node_visits": sh_v, "shadow_prim_tests": sh_p}},
+            "clocks": clk, "wall_s": wall}
+    if not args.no_extras:
+        lctx, lb = bench_lbvh(pt, abi, scenes, torch, 2, 5)
+        lb_bytes = 252 * LBVH_N
+        lb_ach = lb_bytes / (lb["ms"] / 1e3) / 1e9
+        lb["roofline"] = {"bound": "hbm", "achieved": lb_ach, "peak": hbm_peak, "unit": "GB/s",
+                          "frac": lb_ach / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                          "model": "252 B/triangle"}
+        line["lbvh"] = lb
+        line["closest_hit"] = bench_closest(lctx, torch, scenes, 1, 3)
+        lctx.close()
+        if rank == 0:
+            v, cores, desc = CpuReference(shapes, lc, cam, target_s=args.ref_seconds).sample()
+            line["cpu_baseline"] = {"value": v, "unit": "Msamples/s", "cores": cores,
+                                    "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -175,6 +175,11 @@ int  ptgpu_reset_accumulation(ptgpu_ctx *ctx);
 int  ptgpu_draw_frame(ptgpu_ctx *ctx, uint32_t passes, const uint32_t **pixels_out);
 /* Enqueues `passes` passes without any host copy (device-resident timing). */
 int  ptgpu_render_async(ptgpu_ctx *ctx, uint32_t passes);
+/* Runs `passes` passes like ptgpu_render_async with traversal counters on and
+ * synchronises: stats[0..5] = extension node visits, extension primitive
+ * tests, shadow node visits, shadow primitive tests, extension queries,
+ * shadow queries.  For the benchmark's bytes-moved model. */
+int  ptgpu_render_stats(ptgpu_ctx *ctx, uint32_t passes, uint64_t *stats);
 int  ptgpu_synchronize(ptgpu_ctx *ctx);
 /* The float accumulation buffer `colors` (W*H Vec, row-flipped as in
  * RadianceGPU) and the packed pixels. */

@@ -62,7 +62,7 @@ def lib():
         L.orc_generate_camera_ray.argtypes = [vp, vp, vp, i32, i32, i32, i32, vp]
         L.orc_trace_closest.argtypes = [vp, u32, vp, vp, u32, vp, vp, vp, vp, i32]
         L.orc_render_pass.argtypes = [vp, u32, u32, vp, i32, i32, vp, i32, i32, i32,
-                                      vp, vp, vp, i32, i32, i32]
+                                      vp, vp, vp, i32, i32, i32, i32, i32]
         L.orc_lbvh_morton.argtypes = [vp, u32]
         L.orc_sort_desc_stable.argtypes = [vp, u32, vp]
         L.orc_bubblesort_desc.argtypes = [vp, u32, vp]
@@ -78,6 +78,7 @@ def lib():
         L.orc_kd_heap.restype = i32
         L.orc_kd_heap.argtypes = [ctypes.POINTER(KdTree), vp, i32, vp]
         L.orc_to_int.restype = u32
+        L.orc_set_portable_trig.argtypes = [i32]
         L.orc_to_int.argtypes = [f32]
         _lib = L
     return _lib
@@ -197,8 +198,11 @@ def trace_closest(shapes, rays, accel=None, threads=0, count=False):
 
 
 def render(shapes, light_cnt, cam, w, h, seeds, passes, accel=None, max_depth=6,
-           arg_order_rtl=False, colors=None, start_sample=0, threads=0, rows=None):
-    """Runs `passes` RadianceGPU passes; returns (colors, pixels, seeds)."""
+           arg_order_rtl=False, colors=None, start_sample=0, threads=0, rows=None,
+           portable_trig=False, cols=None):
+    """Runs `passes` RadianceGPU passes; returns (colors, pixels, seeds).
+    portable_trig selects the GPU library's own sin/cos instead of libm."""
+    lib().orc_set_portable_trig(1 if portable_trig else 0)
     shapes = abi.as_struct(shapes, abi.SHAPE)
     cam = np.array(cam, abi.CAMERA).reshape(1)
     seeds = np.array(seeds, np.uint32, copy=True)
@@ -207,10 +211,11 @@ def render(shapes, light_cnt, cam, w, h, seeds, passes, accel=None, max_depth=6,
     pixels = np.zeros(w * h, np.uint32)
     a = accel if accel is not None else make_accel(abi.ACCEL_NONE)
     r0, r1 = rows if rows is not None else (0, h)
+    c0, c1 = cols if cols is not None else (0, w)
     for p in range(passes):
         lib().orc_render_pass(_ptr(shapes), len(shapes), light_cnt, ctypes.byref(a), max_depth,
                               1 if arg_order_rtl else 0, _ptr(cam), w, h, start_sample + p,
-                              _ptr(colors), _ptr(pixels), _ptr(seeds), r0, r1, threads)
+                              _ptr(colors), _ptr(pixels), _ptr(seeds), r0, r1, c0, c1, threads)
     return colors, pixels, seeds
 
 

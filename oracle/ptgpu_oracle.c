@@ -51,6 +51,35 @@ static inline float max2f(float a, float b) { return (a > b) ? a : b; }
 static inline float min3f(float a, float b, float c) { return min2f(min2f(a, b), c); }
 static inline float max3f(float a, float b, float c) { return max2f(max2f(a, b), c); }
 
+
+/* Deterministic sine/cosine used by the GPU library for the light-sphere and
+ * diffuse-bounce angles (arguments in [0, 2*pi)).  Quadrant q = round(x*2/pi);
+ * three-part Cody-Waite reduction r = x - q*pi/2 with pi/2 split as
+ * 1.5703125 (8 significant bits, so q*C1 is exact) + 4.83826792e-4 +
+ * 2.56334407e-12; then the Taylor series of sin to r^9 and cos to r^10 on
+ * [-pi/4, pi/4] (truncation error below 1e-9).  Plain multiplies and adds
+ * in a fixed order, so a CPU build without contraction and the GPU build
+ * (-fmad=false) give identical bits. */
+#define PT_SINCOS_BODY                                                          \
+    float q = floorf(x * 0.636619747f + 0.5f);                                  \
+    float r = ((x - q * 1.5703125f) - q * 4.83826792e-4f) - q * 2.56334407e-12f; \
+    float r2 = r * r;                                                           \
+    float sp = r + r * r2 * (-0.166666672f + r2 * (0.00833333377f +             \
+               r2 * (-0.000198412701f + r2 * 2.75573188e-06f)));                \
+    float cp = 1.f + r2 * (-0.5f + r2 * (0.0416666679f + r2 * (-0.00138888892f + \
+               r2 * (2.48015876e-05f + r2 * -2.75573200e-07f))));               \
+    int qi = ((int)q) & 3;                                                      \
+    float sv = (qi == 0) ? sp : (qi == 1) ? cp : (qi == 2) ? -sp : -cp;          \
+    float cv = (qi == 0) ? cp : (qi == 1) ? -sp : (qi == 2) ? -cp : sp;
+
+static int g_portable_trig = 0;
+void orc_set_portable_trig(int on) { g_portable_trig = on; }
+static inline void orc_sincos(float x, float *s, float *c) {
+    if (!g_portable_trig) { *s = sinf(x); *c = cosf(x); return; }
+    PT_SINCOS_BODY
+    *s = sv; *c = cv;
+}
+
 /* ------------------------------------------------------------------------- */
 /* RNG: include/simplernd.h:35-49, rendering_kernel.cl:4-17                    */
 /* ------------------------------------------------------------------------- */
@@ -319,7 +348,9 @@ static void sample_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_
             const float zz = 1.f - 2.f * u1;
             const float rr = sqrtf(fmaxf(0.f, 1.f - zz * zz));
             const float phi = 2.f * ORC_PI * u2;
-            ptgpu_vec unit = v3(rr * cosf(phi), rr * sinf(phi), zz);
+            float sphi, cphi;
+            orc_sincos(phi, &sphi, &cphi);
+            ptgpu_vec unit = v3(rr * cphi, rr * sphi, zz);
             lp = vadd(vsmul(light->g.s.rad, unit), light->g.s.p);
             ln = unit;
         }
@@ -385,8 +416,10 @@ void orc_radiance(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
             ptgpu_vec a = (fabsf(w.x) > .1f) ? v3(0.f, 1.f, 0.f) : v3(1.f, 0.f, 0.f);
             ptgpu_vec u = vnorm(vcross(a, w));
             ptgpu_vec v = vcross(w, u);
-            u = vsmul(cosf(r1) * r2s, u);
-            v = vsmul(sinf(r1) * r2s, v);
+            float sr1, cr1;
+            orc_sincos(r1, &sr1, &cr1);
+            u = vsmul(cr1 * r2s, u);
+            v = vsmul(sr1 * r2s, v);
             ptgpu_vec nd = vadd(u, v);
             w = vsmul(sqrtf(1.f - r2), w);
             nd = vadd(nd, w);
@@ -444,8 +477,10 @@ void orc_render_pass(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
                      const orc_accel *acc, int max_depth, int rtl,
                      const ptgpu_camera *cam, int w, int h, int current_sample,
                      ptgpu_vec *colors, uint32_t *pixels, uint32_t *seeds,
-                     int row_begin, int row_end, int threads) {
+                     int row_begin, int row_end, int col_begin, int col_end, int threads) {
     if (row_end > h) row_end = h;
+    if (col_end > w || col_end <= 0) col_end = w;
+    if (col_begin < 0) col_begin = 0;
 #ifdef _OPENMP
     if (threads <= 0) threads = omp_get_max_threads();
     #pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
@@ -453,7 +488,7 @@ void orc_render_pass(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
     (void)threads;
 #endif
     for (int y = row_begin; y < row_end; ++y) {
-        for (int x = 0; x < w; ++x) {
+        for (int x = col_begin; x < col_end; ++x) {
             const int gid = y * w + x;
             uint32_t s0 = seeds[2 * gid], s1 = seeds[2 * gid + 1];
             ptgpu_ray ray;

@@ -65,8 +65,11 @@ void  orc_render_pass(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
                       const orc_accel *acc, int max_depth, int arg_order_rtl,
                       const ptgpu_camera *cam, int w, int h, int current_sample,
                       ptgpu_vec *colors, uint32_t *pixels, uint32_t *seeds,
-                      int row_begin, int row_end, int threads);
+                      int row_begin, int row_end, int col_begin, int col_end, int threads);
 uint32_t orc_to_int(float x);
+/* 0: sin/cos from libm (as the reference source compiled here); 1: the
+ * library's own deterministic sin/cos (as the GPU computes them) */
+void  orc_set_portable_trig(int on);
 
 /* LBVH */
 void  orc_lbvh_morton(ptgpu_shape *shapes, uint32_t n);

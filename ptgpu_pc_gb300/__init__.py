@@ -24,7 +24,7 @@ EXPORTS = [
     "ptgpu_make_seeds", "ptgpu_set_seeds", "ptgpu_get_seeds", "ptgpu_reset_accumulation",
     "ptgpu_draw_frame", "ptgpu_render_async", "ptgpu_synchronize", "ptgpu_get_colors",
     "ptgpu_get_pixels", "ptgpu_get_current_sample", "ptgpu_trace_closest",
-    "ptgpu_trace_closest_device", "ptgpu_get_stream",
+    "ptgpu_trace_closest_device", "ptgpu_get_stream", "ptgpu_render_stats",
 ]
 
 _lib = None
@@ -80,6 +80,7 @@ def lib():
         L.ptgpu_trace_closest.argtypes = [vp, vp, u32, vp, vp, vp]
         L.ptgpu_trace_closest_device.argtypes = [vp, vp, u32, vp, vp, vp]
         L.ptgpu_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+        L.ptgpu_render_stats.argtypes = [vp, u32, vp]
         _lib = L
     return _lib
 
@@ -230,6 +231,11 @@ class Context:
 
     def render_async(self, passes):
         _check(lib().ptgpu_render_async(self._h, passes))
+
+    def render_stats(self, passes):
+        st = np.zeros(6, np.uint64)
+        _check(lib().ptgpu_render_stats(self._h, passes, _p(st)))
+        return st
 
     def synchronize(self):
         _check(lib().ptgpu_synchronize(self._h))

@@ -536,7 +536,7 @@ int ptgpu_get_current_sample(ptgpu_ctx *c, int32_t *cs) {
     return PTGPU_OK;
 }
 
-static int enqueue_render(ptgpu_ctx *c, uint32_t passes) {
+static int enqueue_render(ptgpu_ctx *c, uint32_t passes, unsigned long long *stats = nullptr) {
     if (c->accel_built < 0) return fail(PTGPU_E_STATE, "build an acceleration structure first");
     if (!c->cam_set) return fail(PTGPU_E_STATE, "set a camera first");
     if (passes == 0) return PTGPU_OK;
@@ -557,6 +557,7 @@ static int enqueue_render(ptgpu_ctx *c, uint32_t passes) {
     a.colors = c->d_colors.as<ptgpu_vec>();
     a.pixels = c->d_pixels.as<uint32_t>();
     a.seeds = c->d_seeds.as<uint32_t>();
+    a.stats = stats;
     CK(launch_render(a, c->block, c->stream));
     c->current_sample += (int)passes;
     return PTGPU_OK;
@@ -589,6 +590,22 @@ int ptgpu_render_async(ptgpu_ctx *c, uint32_t passes) {
     if (!c) return fail(PTGPU_E_INVAL, "null context");
     cudaSetDevice(c->device);
     return enqueue_render(c, passes);
+}
+
+int ptgpu_render_stats(ptgpu_ctx *c, uint32_t passes, uint64_t *stats) {
+    if (!c || !stats) return fail(PTGPU_E_INVAL, "null argument");
+    cudaSetDevice(c->device);
+    unsigned long long *d = nullptr;
+    CK(cudaMalloc(&d, 6 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemsetAsync(d, 0, 6 * sizeof(unsigned long long), c->stream);
+    int st = e == cudaSuccess ? enqueue_render(c, passes, d) : cuda_fail(e, "memset stats");
+    if (st == PTGPU_OK) {
+        e = cudaMemcpyAsync(stats, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) st = cuda_fail(e, "read stats");
+    }
+    cudaFree(d);
+    return st;
 }
 
 int ptgpu_synchronize(ptgpu_ctx *c) {

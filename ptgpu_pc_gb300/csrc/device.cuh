@@ -41,6 +41,32 @@ __device__ __forceinline__ float cl_clamp(float x, float lo, float hi) { return 
 __host__ __device__ __forceinline__ float min2f(float a, float b) { return (a < b) ? a : b; }
 __host__ __device__ __forceinline__ float max2f(float a, float b) { return (a > b) ? a : b; }
 
+
+/* Deterministic sine/cosine used by the GPU library for the light-sphere and
+ * diffuse-bounce angles (arguments in [0, 2*pi)).  Quadrant q = round(x*2/pi);
+ * three-part Cody-Waite reduction r = x - q*pi/2 with pi/2 split as
+ * 1.5703125 (8 significant bits, so q*C1 is exact) + 4.83826792e-4 +
+ * 2.56334407e-12; then the Taylor series of sin to r^9 and cos to r^10 on
+ * [-pi/4, pi/4] (truncation error below 1e-9).  Plain multiplies and adds
+ * in a fixed order, so a CPU build without contraction and the GPU build
+ * (-fmad=false) give identical bits. */
+#define PT_SINCOS_BODY                                                          \
+    float q = floorf(x * 0.636619747f + 0.5f);                                  \
+    float r = ((x - q * 1.5703125f) - q * 4.83826792e-4f) - q * 2.56334407e-12f; \
+    float r2 = r * r;                                                           \
+    float sp = r + r * r2 * (-0.166666672f + r2 * (0.00833333377f +             \
+               r2 * (-0.000198412701f + r2 * 2.75573188e-06f)));                \
+    float cp = 1.f + r2 * (-0.5f + r2 * (0.0416666679f + r2 * (-0.00138888892f + \
+               r2 * (2.48015876e-05f + r2 * -2.75573200e-07f))));               \
+    int qi = ((int)q) & 3;                                                      \
+    float sv = (qi == 0) ? sp : (qi == 1) ? cp : (qi == 2) ? -sp : -cp;          \
+    float cv = (qi == 0) ? cp : (qi == 1) ? -sp : (qi == 2) ? -cp : sp;
+__device__ __forceinline__ void pt_sincos(float x, float &s, float &c) {
+    PT_SINCOS_BODY
+    s = sv;
+    c = cv;
+}
+
 // GetRandom (rendering_kernel.cl:4-17, simplernd.h:35-49)
 __device__ __forceinline__ float get_random(uint32_t &s0, uint32_t &s1) {
     s0 = 36969u * (s0 & 65535u) + (s0 >> 16);
@@ -114,8 +140,13 @@ __device__ __forceinline__ bool enter_box(bool hit, float tmin, float tmax, floa
 
 // Closest hit: returns 1 when any prim reported a non-zero distance (the
 // reference's `intersected`), t/id/prim of the nearest.  Front-to-back order.
+// COUNT: accumulate node visits (v) and primitive tests (p) into cnt[0..1]
+// (the algorithmic-bytes model of the benchmark).
+struct Counts { uint32_t v, p; };
+
+template <bool COUNT = false>
 __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, float &t,
-                                             int &prim, int &id) {
+                                             int &prim, int &id, Counts *cnt = nullptr) {
     t = kInfT;
     prim = -1;
     id = 0;
@@ -124,6 +155,7 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
     if (tv.accel == PTGPU_ACCEL_NONE) {
         for (int i = tv.n_shapes - 1; i >= 0; --i) {
             float dd = prim_intersect(tv.prims, i, o, d);
+            if (COUNT) cnt->p++;
             if (dd != 0.f && dd < t) { t = dd; prim = i; }
         }
         if (prim >= 0) id = prim;
@@ -146,6 +178,7 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
         if (node_cnt > 0) {
             for (int k = node_ref; k < node_ref + node_cnt; ++k) {
                 float dd = prim_intersect(tv.prims, k, o, d);
+                if (COUNT) cnt->p++;
                 if (dd != 0.f) {
                     hit_any = 1;
                     if (dd < t) { t = dd; prim = k; }
@@ -153,6 +186,7 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
             }
         } else {
             const float4 *nd = tv.nodes + 4 * node_ref;
+            if (COUNT) cnt->v++;
             float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
             int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
             float lt0, lt1, rt0, rt1;
@@ -164,6 +198,7 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
             if (lh && q3.z > 0) {
                 for (int k = q3.x; k < q3.x + q3.z; ++k) {
                     float dd = prim_intersect(tv.prims, k, o, d);
+                if (COUNT) cnt->p++;
                     if (dd != 0.f) { hit_any = 1; if (dd < t) { t = dd; prim = k; } }
                 }
                 lh = false;
@@ -171,6 +206,7 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
             if (rhh && q3.w > 0) {
                 for (int k = q3.y; k < q3.y + q3.w; ++k) {
                     float dd = prim_intersect(tv.prims, k, o, d);
+                if (COUNT) cnt->p++;
                     if (dd != 0.f) { hit_any = 1; if (dd < t) { t = dd; prim = k; } }
                 }
                 rhh = false;
@@ -196,12 +232,15 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
 
 // IntersectP (rendering_kernel.cl:375-395): any hit with 0 < d < maxt among
 // shapes 0..n-2 (the last shape is never tested), accelerated.
-__device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float maxt) {
+template <bool COUNT = false>
+__device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float maxt,
+                                          Counts *cnt = nullptr) {
     const int skip = tv.n_shapes - 1;
     if (tv.n_shapes <= 1) return false;
     if (tv.accel == PTGPU_ACCEL_NONE) {
         for (int i = tv.n_shapes - 2; i >= 0; --i) {
             float dd = prim_intersect(tv.prims, i, o, d);
+            if (COUNT) cnt->p++;
             if (dd != 0.f && dd < maxt) return true;
         }
         return false;
@@ -221,10 +260,12 @@ __device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float
             for (int k = node_ref; k < node_ref + node_cnt; ++k) {
                 if (__ldg(&tv.prim_id[k]) == skip) continue;
                 float dd = prim_intersect(tv.prims, k, o, d);
+                if (COUNT) cnt->p++;
                 if (dd != 0.f && dd < maxt) return true;
             }
         } else {
             const float4 *nd = tv.nodes + 4 * node_ref;
+            if (COUNT) cnt->v++;
             float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
             int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
             float lt0, lt1, rt0, rt1;
@@ -234,6 +275,7 @@ __device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float
                 for (int k = q3.x; k < q3.x + q3.z; ++k) {
                     if (__ldg(&tv.prim_id[k]) == skip) continue;
                     float dd = prim_intersect(tv.prims, k, o, d);
+                if (COUNT) cnt->p++;
                     if (dd != 0.f && dd < maxt) return true;
                 }
                 lh = false;
@@ -242,6 +284,7 @@ __device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float
                 for (int k = q3.y; k < q3.y + q3.w; ++k) {
                     if (__ldg(&tv.prim_id[k]) == skip) continue;
                     float dd = prim_intersect(tv.prims, k, o, d);
+                if (COUNT) cnt->p++;
                     if (dd != 0.f && dd < maxt) return true;
                 }
                 rhh = false;

@@ -62,6 +62,7 @@ struct RenderArgs {
     ptgpu_vec *colors;          // W*H, row-flipped (RadianceGPU)
     uint32_t *pixels;           // W*H RGBA8
     uint32_t *seeds;            // 2*W*H
+    unsigned long long *stats;  // optional traversal counters (6 words)
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,

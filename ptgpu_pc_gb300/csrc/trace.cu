@@ -31,8 +31,9 @@ __global__ void k_trace_closest(TraceView tv, const ptgpu_ray *__restrict__ rays
 }
 
 // SampleLights (rendering_kernel.cl:397-493) over the emitter list
+template <bool COUNT>
 __device__ __forceinline__ f3 sample_lights(const RenderArgs &a, uint32_t &s0, uint32_t &s1,
-                                            f3 hit, f3 normal) {
+                                            f3 hit, f3 normal, Counts *cnt) {
     f3 result = mk3(0.f, 0.f, 0.f);
     for (int li = 0; li < a.n_lights; ++li) {
         const LightRec L = a.lights[li];
@@ -51,7 +52,9 @@ __device__ __forceinline__ f3 sample_lights(const RenderArgs &a, uint32_t &s0, u
             const float zz = 1.f - 2.f * u1;
             const float rr = sqrtf(fmaxf(0.f, 1.f - zz * zz));
             const float phi = 2.f * kPi * u2;
-            f3 unit = mk3(rr * cosf(phi), rr * sinf(phi), zz);
+            float sphi, cphi;
+            pt_sincos(phi, sphi, cphi);
+            f3 unit = mk3(rr * cphi, rr * sphi, zz);
             lp = add3(smul3(L.b.x, unit), mk3(L.a.x, L.a.y, L.a.z));
             ln = unit;
         }
@@ -63,7 +66,8 @@ __device__ __forceinline__ f3 sample_lights(const RenderArgs &a, uint32_t &s0, u
         wo = -wo;
         wo = cl_clamp(wo, 0.f, 1.f);
         const float wi = dot3(sd, normal);
-        if (wi > 0.f && !trace_any(a.tv, hit, sd, len - kEps)) {
+        if (COUNT && wi > 0.f) cnt[2].v++;   // shadow query issued
+        if (wi > 0.f && !trace_any<COUNT>(a.tv, hit, sd, len - kEps, cnt + 1)) {
             const float s = L.b.w * wi * wo / (len * len);
             result = add3(result, smul3(s, mk3(L.e.x, L.e.y, L.e.z)));
         }
@@ -72,15 +76,17 @@ __device__ __forceinline__ f3 sample_lights(const RenderArgs &a, uint32_t &s0, u
 }
 
 // RadiancePathTracing + RadianceOnePathTracing (rendering_kernel.cl:495-820)
+template <bool COUNT>
 __device__ __forceinline__ f3 radiance(const RenderArgs &a, f3 o, f3 d, uint32_t &s0,
-                                       uint32_t &s1) {
+                                       uint32_t &s1, Counts *cnt) {
     f3 rad = mk3(0.f, 0.f, 0.f);
     f3 tp = mk3(1.f, 1.f, 1.f);
     int specular = 1;
     for (int depth = 0; depth <= a.max_depth; ++depth) {
         float t;
         int prim, id;
-        if (!trace_closest(a.tv, o, d, t, prim, id)) break;
+        if (COUNT) cnt[2].p++;   // extension query issued
+        if (!trace_closest<COUNT>(a.tv, o, d, t, prim, id, cnt)) break;
         f3 hp = add3(o, smul3(t, d));
         const Material m = a.mats[id];
         const int type = __float_as_int(m.e_type.w);
@@ -117,7 +123,7 @@ __device__ __forceinline__ f3 radiance(const RenderArgs &a, f3 o, f3 d, uint32_t
         if (refl == PTGPU_DIFF) {
             specular = 0;
             tp = mul3(tp, col);
-            f3 ld = sample_lights(a, s0, s1, hp, nl);
+            f3 ld = sample_lights<COUNT>(a, s0, s1, hp, nl, cnt);
             ld = mul3(ld, tp);
             rad = add3(rad, ld);
             float r1 = 2.f * kPi * get_random(s0, s1);
@@ -127,8 +133,10 @@ __device__ __forceinline__ f3 radiance(const RenderArgs &a, f3 o, f3 d, uint32_t
             f3 av = (fabsf(w.x) > .1f) ? mk3(0.f, 1.f, 0.f) : mk3(1.f, 0.f, 0.f);
             f3 u = norm3(cross3(av, w));
             f3 v = cross3(w, u);
-            u = smul3(cosf(r1) * r2s, u);
-            v = smul3(sinf(r1) * r2s, v);
+            float sr1, cr1;
+            pt_sincos(r1, sr1, cr1);
+            u = smul3(cr1 * r2s, u);
+            v = smul3(sr1 * r2s, v);
             f3 nd = add3(u, v);
             w = smul3(sqrtf(1.f - r2), w);
             nd = add3(nd, w);
@@ -180,7 +188,12 @@ __device__ __forceinline__ uint32_t to_int(float x) {
     return (uint32_t)(int)(powf(cl_clamp(x, 0.f, 1.f), 1.f / 2.2f) * 255.f + .5f);
 }
 
+// COUNT = true: the same kernel, also accumulating into a.stats[6]: extension
+// node visits, prim tests; shadow node visits, prim tests; extension and
+// shadow query counts.
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_render(const RenderArgs a) {
+    Counts cnt[3] = {{0, 0}, {0, 0}, {0, 0}};
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int w = a.width, h = a.height;
     if (gid >= w * h) return;
@@ -207,7 +220,7 @@ __global__ void __launch_bounds__(128) k_render(const RenderArgs a) {
                       cam.x.z * kcx + cam.y.z * kcy + cam.dir.z);
         f3 rorig = add3(smul3(0.1f, rdir), mk3(cam.orig.x, cam.orig.y, cam.orig.z));
         rdir = norm3(rdir);
-        f3 r = radiance(a, rorig, rdir, s0, s1);
+        f3 r = radiance<COUNT>(a, rorig, rdir, s0, s1, cnt);
         if (cs == 0) {
             col = r;
         } else {
@@ -223,13 +236,22 @@ __global__ void __launch_bounds__(128) k_render(const RenderArgs a) {
     a.colors[ci] = out;
     a.pixels[gid] = to_int(col.x) | (to_int(col.y) << 8) | (to_int(col.z) << 16) | 0xff000000u;
     reinterpret_cast<uint2 *>(a.seeds)[gid] = make_uint2(s0, s1);
+    if (COUNT) {
+        atomicAdd(a.stats + 0, (unsigned long long)cnt[0].v);
+        atomicAdd(a.stats + 1, (unsigned long long)cnt[0].p);
+        atomicAdd(a.stats + 2, (unsigned long long)cnt[1].v);
+        atomicAdd(a.stats + 3, (unsigned long long)cnt[1].p);
+        atomicAdd(a.stats + 4, (unsigned long long)cnt[2].p);
+        atomicAdd(a.stats + 5, (unsigned long long)cnt[2].v);
+    }
 }
 
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {
     const int n = a.width * a.height;
     if (n <= 0 || a.passes <= 0) return cudaSuccess;
     if (block <= 0) block = 128;
-    k_render<<<(n + block - 1) / block, block, 0, s>>>(a);
+    if (a.stats) k_render<true><<<(n + block - 1) / block, block, 0, s>>>(a);
+    else k_render<false><<<(n + block - 1) / block, block, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -34,7 +34,8 @@ def _gpu_render(shapes, lc, cam, w, h, seeds, passes, accel, max_depth=0, flags=
     return col, pix, sd
 
 
-def _oracle_render(shapes, lc, cam, w, h, seeds, passes, accel, orc, max_depth=6, rtl=False):
+def _oracle_render(shapes, lc, cam, w, h, seeds, passes, accel, orc, max_depth=6, rtl=False,
+                   portable_trig=True):
     if accel == abi.ACCEL_BVH:
         _, btn, btl, _ = orc.build_bvh(shapes)
         acc = orc.make_accel(accel, btn, btl)
@@ -43,7 +44,7 @@ def _oracle_render(shapes, lc, cam, w, h, seeds, passes, accel, orc, max_depth=6
     else:
         acc = orc.make_accel(accel)
     return orc.render(shapes, lc, _oracle_cam(cam, w, h, orc), w, h, seeds, passes, accel=acc,
-                      max_depth=max_depth, arg_order_rtl=rtl)
+                      max_depth=max_depth, arg_order_rtl=rtl, portable_trig=portable_trig)
 
 
 def _rel_rmse(a, b):
@@ -61,8 +62,10 @@ def test_render_cornell_spheres(accel, built_lib, orc):
     o_col, o_pix, o_sd = _oracle_render(shapes, lc, cam, w, h, seeds, 4, accel, orc)
     assert _rel_rmse(g_col, o_col) < RMSE_TOL
     same = (g_col.view(np.uint8).reshape(-1, 12) == o_col.view(np.uint8).reshape(-1, 12)).all(1)
-    assert same.mean() > 0.9
-    assert (g_pix == o_pix).mean() > 0.98
+    assert same.mean() > 0.999
+    # pixels: the gamma pack uses each platform's powf; channels within 1
+    d = np.abs(g_pix.view(np.uint8).astype(int) - o_pix.view(np.uint8).astype(int))
+    assert d.max() <= 1
 
 
 @pytest.mark.parametrize("accel", [abi.ACCEL_BVH, abi.ACCEL_KDTREE])
