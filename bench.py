@@ -312,7 +312,7 @@ def main():
     st = ctx.render_stats(SPP)
     ext_v, ext_p, sh_v, sh_p, ext_q, sh_q = (int(x) for x in st)
     bytes_frame = (24 + 8) * (ext_q + sh_q) + 60 * (ext_v + sh_v) + 36 * (ext_p + sh_p)
-    avg_ms = dev_s / args.steps
+    avg_ms = dev_s * 1e3 / args.steps
     hbm_peak, peak_kind = peaks()
     achieved = bytes_frame / (avg_ms / 1e3) / 1e9
 

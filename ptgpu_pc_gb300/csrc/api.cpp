@@ -82,7 +82,7 @@ struct ptgpu_ctx {
     int accel_built = -1;
     bool bvh_valid = false;
     DevBuf d_btn, d_btl, d_keys, d_keys_alt, d_keys_tmp, d_vals_alt, d_vals_tmp, d_sorted;
-    DevBuf d_status, d_state, d_tile_bounds;
+    DevBuf d_status, d_state, d_block_bounds, d_arrivals, d_tcount, d_tcost;
     DevBuf d_nodes, d_prims, d_prim_id, d_root_box, d_identity;
     int32_t root_first = 0, root_count = 0;
     KdTree kd;
@@ -206,7 +206,8 @@ int ptgpu_destroy(ptgpu_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf *bufs[] = {&c->d_shapes, &c->d_verts, &c->d_type, &c->d_prims0, &c->d_mats, &c->d_lights,
                       &c->d_btn, &c->d_btl, &c->d_keys, &c->d_keys_alt, &c->d_keys_tmp, &c->d_vals_alt,
-                      &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_tile_bounds,
+                      &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_block_bounds, &c->d_arrivals,
+                      &c->d_tcount, &c->d_tcost,
                       &c->d_nodes, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
@@ -352,7 +353,8 @@ static int ensure_bvh_buffers(ptgpu_ctx *c) {
     CK(c->d_sorted.ensure(n * 4));
     CK(c->d_status.ensure(sort_status_words((int)n) * 4));
     CK(c->d_state.ensure(sizeof(BuildState)));
-    CK(c->d_tile_bounds.ensure(((n + 1023) / 1024) * 6 * sizeof(float)));
+    CK(c->d_block_bounds.ensure(block_bound_count((int)n) * 6 * sizeof(float)));
+    CK(c->d_arrivals.ensure(block_bound_count((int)n) * sizeof(uint32_t)));
     return PTGPU_OK;
 }
 
@@ -376,8 +378,10 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
     if (!c) return fail(PTGPU_E_INVAL, "null context");
     if (c->n == 0) return fail(PTGPU_E_STATE, "no shapes set");
     if (accel < 0 || accel > 2) return fail(PTGPU_E_INVAL, "accel must be 0, 1 or 2");
-    if (flags & (PTGPU_FLAG_MORTON_DELTA | PTGPU_FLAG_TREELET))
+    if (flags & PTGPU_FLAG_MORTON_DELTA)
         return fail(PTGPU_E_INVAL, "build flag not supported by this build");
+    if ((flags & PTGPU_FLAG_TREELET) && accel != PTGPU_ACCEL_BVH)
+        return fail(PTGPU_E_INVAL, "treelet restructuring applies to the BVH only");
     cudaSetDevice(c->device);
     c->accel_built = -1;
     c->current_sample = 0;
@@ -400,11 +404,18 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
         b.sorted = c->d_sorted.as<int32_t>();
         b.status = c->d_status.as<uint32_t>();
         b.state = c->d_state.as<BuildState>();
-        b.tile_bounds = c->d_tile_bounds.as<float>();
+        b.block_bounds = c->d_block_bounds.as<float>();
+        b.arrivals = c->d_arrivals.as<uint32_t>();
         b.btn = c->d_btn.as<ptgpu_bvh_node>();
         b.btl = c->d_btl.as<ptgpu_bvh_node>();
         CK(cudaEventRecord(c->ev0, c->stream));
         CK(launch_lbvh_build(b, (int)c->n, c->all_tri ? 1 : 0, c->sm_count, c->stream));
+        if (flags & PTGPU_FLAG_TREELET) {
+            CK(c->d_tcount.ensure((c->n > 1 ? c->n - 1 : 1) * sizeof(int)));
+            CK(c->d_tcost.ensure((c->n > 1 ? c->n - 1 : 1) * sizeof(float)));
+            CK(launch_treelet(b.btn, b.btl, (int)c->n, c->d_tcount.as<int>(), c->d_tcost.as<float>(),
+                              1, c->stream));
+        }
         CK(cudaEventRecord(c->ev1, c->stream));
         BuildState hs;
         CK(cudaMemcpyAsync(&hs, c->d_state.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));

@@ -2,18 +2,18 @@
 //
 // Pipeline (reference mode, all on one stream):
 //   k_centroid_bounds   centroid min/max over all shapes (CLBVH.cpp:91-123)
-//   k_morton_hist       30-bit Morton keys (CLBVH.cpp:125-164) + the digit
-//                       histograms of all four radix passes
+//   k_morton            30-bit Morton keys (CLBVH.cpp:125-164)
+//   k_hist4             digit histograms of all four radix passes
 //   k_onesweep x4       stable LSD radix sort of ~key (== the descending
 //                       stable bubble sort, CLBVH.cpp:31-47), 8-bit digits,
 //                       warp-level ranking, decoupled look-back with a
 //                       bounded spin
 //   k_tiles             per 1024-leaf tile: leaf records + every internal node
 //                       inside the tile, bounds by an in-shared-memory
-//                       bottom-up reduction (kernelConstructRadixTree and
+//                       bottom-up reduction, then a climb over the tiles for
+//                       the nodes above them (kernelConstructRadixTree and
 //                       kernelConstructBVHTree, BVH.cl:141-258, with the
 //                       closed-form topology of lbvh_topo.cuh)
-//   k_top               the internal nodes above the tiles
 // The result is the reference's btn[N-1]/btl[N] arrays, resident on the
 // device.  k_abi_to_trace then derives the 64-byte traversal nodes.
 #include <cfloat>
@@ -172,39 +172,67 @@ __device__ __forceinline__ uint32_t morton30(uint32_t a, uint32_t b, uint32_t c)
     return code;
 }
 
-// Morton keys + per-pass digit histograms.  The sort key is ~code so an
-// ascending stable sort gives the reference's descending stable order.
-__global__ void __launch_bounds__(256) k_morton_hist(const float *__restrict__ verts,
-                                                      const uint8_t *__restrict__ type,
-                                                      int all_tri, int n, BuildState *st,
-                                                      uint32_t *__restrict__ keys) {
+// Morton keys.  The sort key is ~code, so an ascending stable sort gives the
+// reference's descending stable order.  Blocks walk the shapes from the end
+// back to the start: the tail of the array, read last by k_centroid_bounds,
+// is still in L2 when this kernel starts.
+__global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
+                                                 const uint8_t *__restrict__ type, int all_tri,
+                                                 int n, const BuildState *st,
+                                                 uint32_t *__restrict__ keys) {
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) { lo[a] = ord2f(st->cmin[a]); hi[a] = ord2f(st->cmax[a]); }
+    const int nblocks = (n + 255) / 256;
+    for (int blk = nblocks - 1 - (int)blockIdx.x; blk >= 0; blk -= gridDim.x) {
+        int i = blk * 256 + threadIdx.x;
+        if (i >= n) continue;
+        bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
+        f3 p = shape_centroid(verts, i, tri);
+        uint32_t qa = quantise10(p.x, lo[0], hi[0]);
+        uint32_t qb = quantise10(p.y, lo[1], hi[1]);
+        uint32_t qc = quantise10(p.z, lo[2], hi[2]);
+        keys[i] = ~morton30(qa & 1023u, qb & 1023u, qc & 1023u);
+    }
+}
+
+// Digit histograms of all four passes.  Each thread counts runs of equal
+// digits over 16 consecutive keys before touching shared memory, so the
+// long runs of spatially coherent keys cost one atomic each.
+constexpr int kHistItems = 16;
+__global__ void __launch_bounds__(256) k_hist4(const uint32_t *__restrict__ keys, int n,
+                                                BuildState *st) {
     __shared__ uint32_t s_hist[4][256];
     for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
     __syncthreads();
-    float lo[3], hi[3];
-    for (int a = 0; a < 3; ++a) { lo[a] = ord2f(st->cmin[a]); hi[a] = ord2f(st->cmax[a]); }
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        int i = base + threadIdx.x;
-        bool valid = i < n;
-        uint32_t key = 0;
-        if (valid) {
-            bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
-            f3 p = shape_centroid(verts, i, tri);
-            uint32_t qa = quantise10(p.x, lo[0], hi[0]);
-            uint32_t qb = quantise10(p.y, lo[1], hi[1]);
-            uint32_t qc = quantise10(p.z, lo[2], hi[2]);
-            key = ~morton30(qa & 1023u, qb & 1023u, qc & 1023u);
-            keys[i] = key;
-        }
-        unsigned vm = __ballot_sync(0xffffffffu, valid);
-        if (valid) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x * kHistItems;
+    for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kHistItems; base < n;
+         base += stride) {
+        uint32_t k[kHistItems];
+        if (base + kHistItems <= n) {
+            const uint4 *p = reinterpret_cast<const uint4 *>(keys + base);
 #pragma unroll
-            for (int d = 0; d < 4; ++d) {
-                uint32_t dig = (key >> (8 * d)) & 255u;
-                unsigned peers = __match_any_sync(vm, dig);
-                if (lane == __ffs(peers) - 1) atomicAdd(&s_hist[d][dig], (uint32_t)__popc(peers));
+            for (int q = 0; q < kHistItems / 4; ++q) {
+                uint4 v = p[q];
+                k[4 * q] = v.x; k[4 * q + 1] = v.y; k[4 * q + 2] = v.z; k[4 * q + 3] = v.w;
             }
+        } else {
+#pragma unroll
+            for (int q = 0; q < kHistItems; ++q) k[q] = base + q < n ? keys[base + q] : 0u;
+        }
+        const int cnt = (int)min((int64_t)kHistItems, (int64_t)n - base);
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            uint32_t cur = (k[0] >> (8 * d)) & 255u, run = 1;
+#pragma unroll
+            for (int q = 1; q < kHistItems; ++q) {
+                if (q >= cnt) break;
+                uint32_t dg = (k[q] >> (8 * d)) & 255u;
+                if (dg == cur) { ++run; continue; }
+                atomicAdd(&s_hist[d][cur], run);
+                cur = dg;
+                run = 1;
+            }
+            atomicAdd(&s_hist[d][cur], run);
         }
     }
     __syncthreads();
@@ -374,10 +402,21 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__res
 
 // ---------------------------------------------------------------------------
 // emission + refit
+//
+// One CTA per 1024-leaf tile.  Leaves: gather the sorted shape's vertices,
+// compute its bound, stage the 60-byte leaf records in shared memory and
+// copy them out as coalesced words.  Internal nodes whose range lies inside
+// the tile: merge the bounds level by level in shared memory (left then
+// right, as merge_bounds does), stage their records and copy out the ones the
+// tile owns.  The nodes above the tiles are emitted by a climb: the tile's
+// bound goes to a per-level array, and of the two tiles (then blocks) under
+// a parent the one that arrives second merges them and moves up.
 // ---------------------------------------------------------------------------
 constexpr int kTileLeaves = 1024;
 constexpr int kTileLog = 10;
 constexpr int kTileThreads = 512;
+constexpr int kRecWords = 15;
+constexpr size_t kTileSmem = (6 * kTileLeaves) * sizeof(float) + kTileLeaves * kRecWords * 4 + kTileLeaves;
 
 __device__ __forceinline__ void write_node(ptgpu_bvh_node *dst, int mn, int mx, int nshape, int leaf,
                                            int nl, int nr, int np, const float b[6], uint32_t cost_bits,
@@ -385,8 +424,17 @@ __device__ __forceinline__ void write_node(ptgpu_bvh_node *dst, int mn, int mx, 
     int *d = reinterpret_cast<int *>(dst);
     d[0] = mn; d[1] = mx; d[2] = nshape; d[3] = leaf; d[4] = nl; d[5] = nr; d[6] = np;
     float *f = reinterpret_cast<float *>(dst) + 7;
-    f[0] = b[0]; f[1] = b[1]; f[2] = b[2]; f[3] = b[3]; f[4] = b[4]; f[5] = b[5];
+    for (int a = 0; a < 6; ++a) f[a] = b[a];
     d[13] = (int)cost_bits; d[14] = (int)area_bits;
+}
+
+__device__ __forceinline__ void stage_node(uint32_t *rec, int mn, int mx, int nshape, int leaf,
+                                           int nl, int nr, int np, const float b[6],
+                                           uint32_t cost_bits, uint32_t area_bits) {
+    rec[0] = (uint32_t)mn; rec[1] = (uint32_t)mx; rec[2] = (uint32_t)nshape; rec[3] = (uint32_t)leaf;
+    rec[4] = (uint32_t)nl; rec[5] = (uint32_t)nr; rec[6] = (uint32_t)np;
+    for (int a = 0; a < 6; ++a) rec[7 + a] = __float_as_uint(b[a]);
+    rec[13] = cost_bits; rec[14] = area_bits;
 }
 
 __device__ __forceinline__ void merge6(float *a, const float *b) {   // merge_bounds(a, b)
@@ -395,17 +443,24 @@ __device__ __forceinline__ void merge6(float *a, const float *b) {   // merge_bo
     a[4] = min2f(a[4], b[4]); a[5] = max2f(a[5], b[5]);
 }
 
-// emits the record of the node covering block [lo, hi] (right half non-empty)
-__device__ __forceinline__ void emit_internal(ptgpu_bvh_node *btn, int lo, int hi, int level,
-                                              int n, const float b[6]) {
+// record fields of the node covering block [lo, hi] (right half non-empty)
+struct BlockNode { int idx, gamma, parent, leaf; };
+__device__ __forceinline__ BlockNode block_node(int lo, int hi, int level, int n) {
     int32_t a_lo, a_hi, a_g;
     topo_range(lo, n, a_lo, a_hi, a_g);
-    int idx = (a_lo == lo && a_hi == hi) ? lo : hi;
-    if (idx < 0 || idx > n - 2) return;   // unreachable for a valid block; keeps writes in bounds
-    int gamma = lo + (1 << (level - 1)) - 1;
-    bool ll = (level == 1), rl = (hi == gamma + 1);
-    int parent = topo_parent_internal(idx, lo, hi, n);
-    write_node(&btn[idx], lo, hi, 0, (ll || rl) ? 2 : 0, gamma, gamma + 1, parent, b, 0u, 0u);
+    BlockNode r;
+    r.idx = (a_lo == lo && a_hi == hi) ? lo : hi;
+    r.gamma = lo + (1 << (level - 1)) - 1;
+    r.leaf = (level == 1 || hi == r.gamma + 1) ? 2 : 0;
+    r.parent = topo_parent_internal(r.idx, lo, hi, n);
+    return r;
+}
+
+// offset of level `level` (>= kTileLog) in the per-level block arrays
+__device__ __forceinline__ int level_offset(int level, int ntiles) {
+    int off = 0;
+    for (int l = kTileLog; l < level; ++l) off += (ntiles + (1 << (l - kTileLog)) - 1) >> (l - kTileLog);
+    return off;
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_tiles(const float *__restrict__ verts,
@@ -413,76 +468,311 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float *__restrict_
                                                          int all_tri, const int32_t *__restrict__ sorted,
                                                          int n, ptgpu_bvh_node *__restrict__ btn,
                                                          ptgpu_bvh_node *__restrict__ btl,
-                                                         float *__restrict__ tile_bounds) {
-    __shared__ float sb[6][kTileLeaves];
+                                                         float *__restrict__ block_bounds,
+                                                         uint32_t *__restrict__ arrivals, int ntiles) {
+    extern __shared__ __align__(16) unsigned char tsm[];
+    float *sb = reinterpret_cast<float *>(tsm);                          // [6][1024]
+    uint32_t *rec = reinterpret_cast<uint32_t *>(sb + 6 * kTileLeaves);  // [1024][15]
+    unsigned char *own = reinterpret_cast<unsigned char *>(rec + kTileLeaves * kRecWords);
     const int T0 = blockIdx.x * kTileLeaves;
     const int cnt = min(kTileLeaves, n - T0);
-    for (int k = threadIdx.x; k < cnt; k += kTileThreads) {
-        int leaf = T0 + k;
-        int s = min(max(sorted[leaf], 0), n - 1);   // in bounds even after a failed sort
-        bool tri = all_tri || type[s] == PTGPU_TRIANGLE;
+    const int tid = threadIdx.x;
+    // ---- leaves
+    for (int k = tid; k < cnt; k += kTileThreads) {
+        const int leaf = T0 + k;
+        const int s = min(max(sorted[leaf], 0), n - 1);   // in bounds even after a failed sort
+        const bool tri = all_tri || type[s] == PTGPU_TRIANGLE;
         float b[6];
         shape_bound(verts, s, tri, b);
-        for (int a = 0; a < 6; ++a) sb[a][k] = b[a];
-        int parent = n >= 2 ? topo_parent_leaf(leaf, n) : -1;
-        write_node(&btl[leaf], -1, -1, s, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
+        for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + k] = b[a];
+        const int parent = n >= 2 ? topo_parent_leaf(leaf, n) : -1;
+        stage_node(rec + k * kRecWords, -1, -1, s, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
+        own[k] = 0;
     }
     __syncthreads();
+    {
+        uint32_t *dst = reinterpret_cast<uint32_t *>(btl + T0);
+        for (int w = tid; w < cnt * kRecWords; w += kTileThreads) dst[w] = rec[w];
+    }
+    __syncthreads();
+    // ---- internal nodes inside the tile
     for (int level = 1; level <= kTileLog; ++level) {
         const int half = 1 << (level - 1);
         const int nblk = (cnt + (1 << level) - 1) >> level;
-        for (int bidx = threadIdx.x; bidx < nblk; bidx += kTileThreads) {
-            int l0 = bidx << level;
-            int r0 = l0 + half;
-            if (r0 < cnt) {
-                float b[6], c[6];
-                for (int a = 0; a < 6; ++a) { b[a] = sb[a][l0]; c[a] = sb[a][r0]; }
-                merge6(b, c);
-                for (int a = 0; a < 6; ++a) sb[a][l0] = b[a];
-                int lo = T0 + l0;
-                int hi = min(T0 + l0 + (1 << level), n) - 1;
-                emit_internal(btn, lo, hi, level, n, b);
-            }
+        for (int bidx = tid; bidx < nblk; bidx += kTileThreads) {
+            const int l0 = bidx << level, r0 = l0 + half;
+            if (r0 >= cnt) continue;                       // right half empty: same set
+            float b[6], c[6];
+            for (int a = 0; a < 6; ++a) { b[a] = sb[a * kTileLeaves + l0]; c[a] = sb[a * kTileLeaves + r0]; }
+            merge6(b, c);
+            for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + l0] = b[a];
+            const int lo = T0 + l0;
+            const int hi = min(T0 + l0 + (1 << level), n) - 1;
+            const BlockNode bn = block_node(lo, hi, level, n);
+            const int j = bn.idx - T0;
+            stage_node(rec + j * kRecWords, lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b,
+                       0u, 0u);
+            own[j] = 1;
         }
         __syncthreads();
     }
-    if (threadIdx.x < 6) tile_bounds[(size_t)blockIdx.x * 6 + threadIdx.x] = sb[threadIdx.x][0];
+    {
+        uint32_t *dst = reinterpret_cast<uint32_t *>(btn + T0);
+        const int last = min(kTileLeaves, n - 1 - T0);     // internal indices < n-1
+        for (int w = tid; w < last * kRecWords; w += kTileThreads)
+            if (own[w / kRecWords]) dst[w] = rec[w];
+    }
+    // ---- climb above the tile (one thread)
+    if (tid != 0 || n <= kTileLeaves) return;
+    float b[6];
+    for (int a = 0; a < 6; ++a) b[a] = sb[a * kTileLeaves];
+    int level = kTileLog;
+    int j = blockIdx.x;                                    // block index at `level`
+    int off = 0;                                           // level_offset(level)
+    for (;;) {
+        float *mine = block_bounds + 6 * (size_t)(off + j);
+        for (int a = 0; a < 6; ++a) mine[a] = b[a];
+        if ((1 << level) >= n) break;                      // this block is the root's
+        const int noff = off + ((ntiles + (1 << (level - kTileLog)) - 1) >> (level - kTileLog));
+        const int pj = j >> 1;
+        const int64_t right_lo = ((int64_t)(2 * pj + 1)) << level;
+        if (right_lo >= n) {                               // parent has no right half
+            level++; j = pj; off = noff;
+            continue;
+        }
+        __threadfence();
+        if (atomicAdd(&arrivals[noff + pj], 1u) == 0u) return;   // sibling not done yet
+        __threadfence();
+        const float *lb = block_bounds + 6 * (size_t)(off + 2 * pj);
+        const float *rb = block_bounds + 6 * (size_t)(off + 2 * pj + 1);
+        for (int a = 0; a < 6; ++a) b[a] = __ldcg(lb + a);
+        float c[6];
+        for (int a = 0; a < 6; ++a) c[a] = __ldcg(rb + a);
+        merge6(b, c);
+        level++;
+        const int lo = (int)((int64_t)pj << level);
+        const int64_t he = (int64_t)lo + ((int64_t)1 << level);
+        const int hi = (int)((he < n ? he : n) - 1);
+        const BlockNode bn = block_node(lo, hi, level, n);
+        write_node(&btn[bn.idx], lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
+        j = pj;
+        off = noff;
+    }
 }
 
-// levels above the tiles: one CTA, bounds of tile-aligned blocks kept in
-// shared memory (global memory when there are more than kTopSmemTiles tiles)
-constexpr int kTopThreads = 1024;
-constexpr int kTopSmemTiles = 4096;
+// ---------------------------------------------------------------------------
+// Treelet restructuring (Karras & Aila, "Fast Parallel Construction of
+// High-Quality Bounding Volume Hierarchies", HPG 2013), the stage that
+// kernelOptimize / treeletOptimize (BVH.cl:291-543) set out to implement:
+// bottom-up over the tree with atomic arrival counters; at each node the
+// treelet of up to 7 leaves is grown by expanding the largest-area child,
+// the optimal binary topology over those leaves is found by dynamic
+// programming over all 127 subsets with SAH cost Ci*A + children (Ci = 1.2,
+// leaf cost Ct*A with Ct = 1.0, clheader.h:14-15), and the treelet is rebuilt
+// in place when that is strictly cheaper.  Internal nodes mark a leaf child
+// with min == nLeft / max == nRight and an internal child with -1.  One
+// thread per treelet; the float operations and their order are those of the
+// oracle's sequential restatement, so the two trees agree byte for byte.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float area6(const float *b) {
+    float dx = b[1] - b[0], dy = b[3] - b[2], dz = b[5] - b[4];
+    return 2.f * (dx * dy + dx * dz + dy * dz);
+}
 
-__global__ void __launch_bounds__(kTopThreads) k_top(float *__restrict__ tile_bounds, int ntiles,
-                                                      int n, ptgpu_bvh_node *__restrict__ btn) {
-    extern __shared__ float tb[];   // [ntiles][6] when it fits
-    const bool in_smem = ntiles <= kTopSmemTiles;
-    float *arr = in_smem ? tb : tile_bounds;
-    if (in_smem)
-        for (int i = threadIdx.x; i < ntiles * 6; i += kTopThreads) tb[i] = tile_bounds[i];
-    __syncthreads();
-    for (int level = kTileLog + 1; (1 << (level - 1)) < n; ++level) {
-        const int step = 1 << (level - kTileLog);        // tiles per block at this level
-        const int halfstep = step >> 1;
-        const int nblk = (ntiles + step - 1) / step;
-        for (int bidx = threadIdx.x; bidx < nblk; bidx += kTopThreads) {
-            int j = bidx * step;
-            int jr = j + halfstep;
-            if (jr < ntiles) {
-                float b[6], c[6];
-                for (int a = 0; a < 6; ++a) { b[a] = arr[j * 6 + a]; c[a] = arr[jr * 6 + a]; }
-                merge6(b, c);
-                for (int a = 0; a < 6; ++a) arr[j * 6 + a] = b[a];
-                int lo = j * kTileLeaves;
-                int64_t he = (int64_t)lo + ((int64_t)1 << level);
-                int hi = (int)((he < n ? he : n) - 1);
-                emit_internal(btn, lo, hi, level, n, b);
+// Nodes and costs written by other threads are read past L1 (ld.global.cg):
+// a node's subtree was finished on another SM before its arrival counter
+// let this thread in.
+struct NodeL {
+    int min, max, leaf, nLeft, nRight, nParent;
+};
+__device__ __forceinline__ NodeL load_node(const ptgpu_bvh_node *btn, int i) {
+    const int *w = reinterpret_cast<const int *>(btn + i);
+    NodeL n;
+    n.min = __ldcg(w + 0); n.max = __ldcg(w + 1); n.leaf = __ldcg(w + 3);
+    n.nLeft = __ldcg(w + 4); n.nRight = __ldcg(w + 5); n.nParent = __ldcg(w + 6);
+    return n;
+}
+__device__ __forceinline__ void ref_bound6(int r, const ptgpu_bvh_node *btn,
+                                           const ptgpu_bvh_node *btl, float *b) {
+    const float *x = reinterpret_cast<const float *>(r < 0 ? btl + (-r - 1) : btn + r) + 7;
+    for (int a = 0; a < 6; ++a) b[a] = __ldcg(x + a);
+}
+
+__device__ __forceinline__ int child_ref(const NodeL &nd, bool right) {
+    if (!right) return nd.nLeft == nd.min ? -(nd.nLeft + 1) : nd.nLeft;
+    return nd.nRight == nd.max ? -(nd.nRight + 1) : nd.nRight;
+}
+
+__device__ __forceinline__ float ref_cost(int r, const float *cost, const ptgpu_bvh_node *btl) {
+    if (r >= 0) return __ldcg(cost + r);
+    float b[6];
+    ref_bound6(r, nullptr, btl, b);
+    return 1.0f * area6(b);
+}
+
+// normalise child marks: min = nLeft for a leaf left child else -1, likewise max
+__global__ void k_treelet_prepare(ptgpu_bvh_node *btn, int n, int *counters) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    ptgpu_bvh_node &p = btn[i];
+    bool ll = p.nLeft == p.min, rl = p.nRight == p.max;
+    p.min = ll ? p.nLeft : -1;
+    p.max = rl ? p.nRight : -1;
+    counters[i] = 0;
+}
+
+__device__ void treelet_at(int root, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, float *cost) {
+    int leaves[7], nodes[6];
+    int nl = 0, nn = 0;
+    {
+        const NodeL r = load_node(btn, root);
+        leaves[nl++] = child_ref(r, false);
+        leaves[nl++] = child_ref(r, true);
+    }
+    while (nl < 7) {
+        int best = -1;
+        float best_a = -1.f;
+        for (int i = 0; i < nl; i++) {
+            if (leaves[i] < 0) continue;
+            float b[6];
+            ref_bound6(leaves[i], btn, btl, b);
+            float a = area6(b);
+            if (a > best_a) { best_a = a; best = i; }
+        }
+        if (best < 0) break;
+        int nd = leaves[best];
+        nodes[nn++] = nd;
+        const NodeL x = load_node(btn, nd);
+        leaves[best] = child_ref(x, false);
+        leaves[nl++] = child_ref(x, true);
+    }
+    if (nl < 3) return;
+    const int nsub = 1 << nl;
+    float lb[7][6];
+    for (int i = 0; i < nl; i++) ref_bound6(leaves[i], btn, btl, lb[i]);
+    float area[128], copt[128];
+    unsigned char popt[128];
+    for (int s = 1; s < nsub; s++) {
+        float b[6];
+        bool first = true;
+        for (int i = 0; i < nl; i++) {
+            if (!((s >> i) & 1)) continue;
+            if (first) { for (int a = 0; a < 6; ++a) b[a] = lb[i][a]; first = false; }
+            else merge6(b, lb[i]);
+        }
+        area[s] = area6(b);
+    }
+    for (int i = 0; i < nl; i++) copt[1 << i] = ref_cost(leaves[i], cost, btl);
+    for (int k = 2; k <= nl; k++) {
+        for (int s = 1; s < nsub; s++) {
+            if (__popc(s) != k) continue;
+            float bestc = FLT_MAX;
+            int bp = 0;
+            int d = (s - 1) & s;
+            int p = (-d) & s;
+            while (p != 0) {
+                float c = copt[p] + copt[s ^ p];
+                if (c < bestc) { bestc = c; bp = p; }
+                p = (p - d) & s;
+            }
+            copt[s] = 1.2f * area[s] + bestc;
+            popt[s] = (unsigned char)bp;
+        }
+    }
+    const int full = nsub - 1;
+    if (!(copt[full] < __ldcg(cost + root))) return;
+    int slots[7];
+    int ns = 0;
+    slots[ns++] = root;
+    for (int i = 0; i < nn; i++) slots[ns++] = nodes[i];
+    int used = 0;
+    int st_s[16], st_n[16], top = 0;
+    st_s[top] = full; st_n[top] = slots[used++]; top++;
+    while (top) {
+        top--;
+        int s = st_s[top], nd = st_n[top];
+        int ls = popt[s], rs = s ^ ls;
+        int refs[2];
+        int subs[2] = {ls, rs};
+        for (int c = 0; c < 2; c++) {
+            if (__popc(subs[c]) == 1) {
+                refs[c] = leaves[__ffs(subs[c]) - 1];
+            } else {
+                refs[c] = slots[used++];
+                st_s[top] = subs[c]; st_n[top] = refs[c]; top++;
             }
         }
-        if (!in_smem) __threadfence_block();
-        __syncthreads();
+        ptgpu_bvh_node &p = btn[nd];
+        p.nLeft = refs[0] < 0 ? -refs[0] - 1 : refs[0];
+        p.nRight = refs[1] < 0 ? -refs[1] - 1 : refs[1];
+        p.min = refs[0] < 0 ? p.nLeft : -1;
+        p.max = refs[1] < 0 ? p.nRight : -1;
+        p.leaf = (refs[0] < 0 || refs[1] < 0) ? 2 : 0;
+        if (refs[0] < 0) btl[-refs[0] - 1].nParent = nd; else btn[refs[0]].nParent = nd;
+        if (refs[1] < 0) btl[-refs[1] - 1].nParent = nd; else btn[refs[1]].nParent = nd;
     }
+    __threadfence();
+    for (int i = used - 1; i >= 0; i--) {
+        int nd = slots[i];
+        ptgpu_bvh_node &p = btn[nd];
+        const NodeL q = load_node(btn, nd);
+        int lr = q.min == q.nLeft ? -(q.nLeft + 1) : q.nLeft;
+        int rr = q.max == q.nRight ? -(q.nRight + 1) : q.nRight;
+        float b[6], c[6];
+        ref_bound6(lr, btn, btl, b);
+        ref_bound6(rr, btn, btl, c);
+        merge6(b, c);
+        p.bound.min_x = b[0]; p.bound.max_x = b[1]; p.bound.min_y = b[2];
+        p.bound.max_y = b[3]; p.bound.min_z = b[4]; p.bound.max_z = b[5];
+        cost[nd] = 1.2f * area6(b) + ref_cost(lr, cost, btl) + ref_cost(rr, cost, btl);
+        __threadfence();
+    }
+}
+
+__global__ void __launch_bounds__(128) k_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n,
+                                                  int *counters, float *cost) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int node = btl[k].nParent;
+    while (node >= 0 && node < n - 1) {
+        __threadfence();
+        if (atomicAdd(&counters[node], 1) == 0) return;    // the second arrival goes on
+        __threadfence();
+        // all of node's subtree is final: compute its cost, then restructure
+        {
+            const NodeL p = load_node(btn, node);
+            int lr = p.min == p.nLeft ? -(p.nLeft + 1) : p.nLeft;
+            int rr = p.max == p.nRight ? -(p.nRight + 1) : p.nRight;
+            float b[6];
+            ref_bound6(node, btn, btl, b);
+            cost[node] = 1.2f * area6(b) + ref_cost(lr, cost, btl) + ref_cost(rr, cost, btl);
+        }
+        treelet_at(node, btn, btl, cost);
+        if (node == 0) return;
+        node = load_node(btn, node).nParent;
+    }
+}
+
+__global__ void k_treelet_finish(ptgpu_bvh_node *btn, int n, const float *cost) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    ptgpu_bvh_node &p = btn[i];
+    float b[6] = {p.bound.min_x, p.bound.max_x, p.bound.min_y, p.bound.max_y, p.bound.min_z,
+                  p.bound.max_z};
+    p.cost = cost[i];
+    p.area = area6(b);
+}
+
+cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int *counters,
+                           float *cost, int sweeps, cudaStream_t s) {
+    if (n < 3) return cudaSuccess;
+    k_treelet_prepare<<<(n + 255) / 256, 256, 0, s>>>(btn, n, counters);
+    for (int it = 0; it < sweeps; ++it) {
+        if (it > 0) cudaMemsetAsync(counters, 0, sizeof(int) * (size_t)(n - 1), s);
+        k_treelet<<<(n + 127) / 128, 128, 0, s>>>(btn, btl, n, counters, cost);
+    }
+    k_treelet_finish<<<(n + 255) / 256, 256, 0, s>>>(btn, n, cost);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -564,28 +854,37 @@ size_t sort_status_words(int n) {
     return tiles * 256 * 4;
 }
 
+size_t block_bound_count(int n) {
+    size_t ntiles = ((size_t)n + kTileLeaves - 1) / kTileLeaves;
+    return 2 * ntiles + 64;
+}
+
 cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_count,
                               cudaStream_t s) {
     if (n < 1) return cudaErrorInvalidValue;
     const int ntiles_sort = (n + kSortTile - 1) / kSortTile;
+    const int ntiles = (n + kTileLeaves - 1) / kTileLeaves;
     cudaError_t e;
-    k_init_state<<<1, 256, 0, s>>>(b.state);
-    e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    const int red_grid = grid_for(n, 256, sm_count * 8);
-    k_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state);
-    k_morton_hist<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state, b.keys);
-    const size_t smem = sizeof(SortSmem);
     static bool attr_set = false;
+    const size_t smem = sizeof(SortSmem);
     if (!attr_set) {
         cudaFuncSetAttribute(k_onesweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_onesweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_onesweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_top, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopSmemTiles * 6 * 4);
+        cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
         attr_set = true;
     }
+    k_init_state<<<1, 256, 0, s>>>(b.state);
+    e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(b.arrivals, 0, block_bound_count(n) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const int red_grid = grid_for(n, 256, sm_count * 8);
+    k_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state);
+    k_morton<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state, b.keys);
+    k_hist4<<<grid_for((n + kHistItems - 1) / kHistItems, 256, sm_count * 4), 256, 0, s>>>(b.keys, n, b.state);
     const size_t pass_words = (size_t)ntiles_sort * 256;
-    // pass 0: keys -> (keys_alt, vals_alt); 1: alt -> main; 2: main -> alt; 3: alt -> sorted
+    // pass 0: keys -> (keys_alt, vals_alt); 1: alt -> tmp; 2: tmp -> alt; 3: alt -> sorted
     k_onesweep<true, false><<<ntiles_sort, kSortThreads, smem, s>>>(
         b.keys, nullptr, b.keys_alt, b.vals_alt, n, 0, b.state, b.status);
     k_onesweep<false, false><<<ntiles_sort, kSortThreads, smem, s>>>(
@@ -594,13 +893,8 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
         b.keys_tmp, b.vals_tmp, b.keys_alt, b.vals_alt, n, 2, b.state, b.status + 2 * pass_words);
     k_onesweep<false, true><<<ntiles_sort, kSortThreads, smem, s>>>(
         b.keys_alt, b.vals_alt, nullptr, b.sorted, n, 3, b.state, b.status + 3 * pass_words);
-    const int ntiles = (n + kTileLeaves - 1) / kTileLeaves;
-    k_tiles<<<ntiles, kTileThreads, 0, s>>>(b.verts, b.type, all_tri, b.sorted, n, b.btn, b.btl,
-                                            b.tile_bounds);
-    if (ntiles > 1) {
-        size_t tsm = ntiles <= kTopSmemTiles ? (size_t)ntiles * 6 * 4 : 0;
-        k_top<<<1, kTopThreads, tsm, s>>>(b.tile_bounds, ntiles, n, b.btn);
-    }
+    k_tiles<<<ntiles, kTileThreads, kTileSmem, s>>>(b.verts, b.type, all_tri, b.sorted, n, b.btn,
+                                                    b.btl, b.block_bounds, b.arrivals, ntiles);
     return cudaGetLastError();
 }
 

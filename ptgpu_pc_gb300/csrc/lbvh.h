@@ -28,16 +28,20 @@ struct LbvhBuffers {
     int32_t *sorted;            // sorted_geometry_indices
     uint32_t *status;           // look-back words, sort_status_words(n)
     BuildState *state;
-    float *tile_bounds;         // 6 floats per 1024-leaf tile
+    float *block_bounds;        // 6 floats per block at the tile level and above
+    uint32_t *arrivals;         // arrival counters of the blocks above the tiles
     ptgpu_bvh_node *btn, *btl;  // the reference's output arrays
 };
 
 size_t sort_status_words(int n);
+size_t block_bound_count(int n);   // blocks at the tile level and above (+ slack)
 
 cudaError_t launch_unpack_shapes(const ptgpu_shape *d_shapes, int n, float *verts, uint8_t *type,
                                  float4 *prims, Material *mats, cudaStream_t s);
 cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_count,
                               cudaStream_t s);
+cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int *counters,
+                           float *cost, int sweeps, cudaStream_t s);
 cudaError_t launch_abi_to_trace(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, int n,
                                 const float4 *prims0, float4 *nodes, float4 *prims,
                                 int32_t *prim_id, cudaStream_t s);

@@ -89,3 +89,39 @@ def test_lbvh_4m_properties(built_lib):
     assert np.array_equal(btn["bound"][:, 0::2], mins)
     assert np.array_equal(btn["bound"][:, 1::2], maxs)
     assert ms > 0
+
+
+@pytest.mark.parametrize("case", ["ico4", "soup", "cornell", "odd"])
+def test_treelet_matches_oracle(case, built_lib, orc):
+    """GPU treelet restructuring == the oracle's sequential restatement, byte
+    for byte; the SAH cost drops; every leaf stays in the tree once."""
+    import ptgpu_pc_gb300 as pt
+    shapes = {"ico4": lambda: scenes.icosphere_scene(level=4)[0],
+              "soup": lambda: scenes.triangle_soup(30000, seed=4),
+              "cornell": lambda: scenes.cornell_spheres()[0],
+              "odd": lambda: scenes.triangle_soup(4097, seed=5)}[case]()
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, 0)
+        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET)
+        g_btn, g_btl = ctx.get_bvh()
+    _, btn, btl, _ = orc.build_bvh(shapes)
+    o_btn, o_btl = orc.treelet_optimize(btn, btl)
+    assert g_btl.tobytes() == o_btl.tobytes()
+    assert g_btn.tobytes() == o_btn.tobytes()
+    if len(shapes) > 2:
+        assert orc.sah_cost(g_btn, g_btl) <= orc.sah_cost(btn, btl) + 1e-9
+
+
+def test_treelet_closest_hits_unchanged(built_lib, orc):
+    import ptgpu_pc_gb300 as pt
+    shapes = scenes.triangle_soup(100_000, seed=14)
+    rays = scenes.random_rays(30_000, seed=15)
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, 0)
+        ctx.build(abi.ACCEL_BVH)
+        a = ctx.trace_closest(rays)
+        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET)
+        b = ctx.trace_closest(rays)
+    assert np.array_equal(a[2], b[2])
+    assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
+    assert (a[1] == b[1]).mean() > 0.9999
