@@ -39,6 +39,7 @@ LBVH_N = 1 << 22
 RAYS_N = 1 << 24
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = "icosphere_81934tri_512x512_16spp_depth8_bvh"
+BUILD_FLAGS = 0x4   # PTGPU_FLAG_TREELET: the 7-leaf treelet stage of the scene's build
 
 
 def peaks():
@@ -265,7 +266,8 @@ def main():
     shapes, lc, cam = scenes.icosphere_scene(level=6)
     ctx = pt.Context(W, H, accel=abi.ACCEL_BVH, max_depth=MAX_DEPTH, device=local)
     ctx.set_shapes(shapes, lc)
-    ctx.build(abi.ACCEL_BVH)
+    ctx.build(abi.ACCEL_BVH, BUILD_FLAGS)     # Morton, sort, Karras, refit, treelets
+    build_ms = ctx.last_build_ms()
     ctx.set_camera(cam)
     seeds = pt.make_seeds(1 + rank, 2 * W * H)
     ctx.set_seeds(seeds)
@@ -322,13 +324,13 @@ def main():
     ctx_e.set_camera(cam)
     h2d = shapes.nbytes + seeds.nbytes
     d2h = W * H * 4
-    ctx_e.set_shapes(shapes, lc); ctx_e.build(abi.ACCEL_BVH); ctx_e.set_seeds(seeds)
+    ctx_e.set_shapes(shapes, lc); ctx_e.build(abi.ACCEL_BVH, BUILD_FLAGS); ctx_e.set_seeds(seeds)
     ctx_e.draw_frame(SPP)                     # warm-up
     barrier(pg)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx_e.set_shapes(shapes, lc)
-        ctx_e.build(abi.ACCEL_BVH)
+        ctx_e.build(abi.ACCEL_BVH, BUILD_FLAGS)
         ctx_e.set_seeds(seeds)
         pix = ctx_e.draw_frame_view(SPP)
     e2e_s = reduce_max(time.perf_counter() - t0, pg, device)
@@ -340,11 +342,12 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded displaced icosphere, 81,934 shapes)",
             "config": {"workload": WORKLOAD, "shapes": int(len(shapes)), "width": W, "height": H,
-                       "spp": SPP, "max_depth": MAX_DEPTH, "accel": "bvh", "l2": "flushed between steps (256 MB write)",
+                       "spp": SPP, "max_depth": MAX_DEPTH, "accel": "bvh", "treelets": True,
+                       "scene_build_ms": build_ms, "l2": "flushed between steps (256 MB write)",
                        "parallelism": "replicas x%d" % world},
             "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-                    "per_step": "set_shapes + BVH build + set_seeds + draw_frame(16)"},
+                    "per_step": "set_shapes + BVH build (with treelets) + set_seeds + draw_frame(16)"},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
