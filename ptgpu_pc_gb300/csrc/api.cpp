@@ -83,7 +83,9 @@ struct ptgpu_ctx {
     bool bvh_valid = false;
     DevBuf d_btn, d_btl, d_keys, d_keys_alt, d_keys_tmp, d_vals_alt, d_vals_tmp, d_sorted;
     DevBuf d_status, d_state, d_block_bounds, d_arrivals, d_tcount, d_tcost;
-    DevBuf d_nodes, d_prims, d_prim_id, d_root_box, d_identity;
+    DevBuf d_nodes, d_nodes4, d_prims, d_prim_id, d_root_box, d_identity;
+    int n_internal = 0;
+    bool wide = true;
     int32_t root_first = 0, root_count = 0;
     KdTree kd;
     bool kd_valid = false;
@@ -114,6 +116,7 @@ static TraceView make_view(ptgpu_ctx *c) {
     }
     tv.accel = c->accel_built;
     tv.nodes = c->d_nodes.as<float4>();
+    tv.nodes4 = (c->wide && c->root_count == 0 && c->n_internal > 0) ? c->d_nodes4.as<float4>() : nullptr;
     tv.prims = c->d_prims.as<float4>();
     tv.prim_id = c->d_prim_id.as<int32_t>();
     tv.root_first = c->root_first;
@@ -168,6 +171,7 @@ int ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out) {
     c->block = cfg->block_size > 0 ? cfg->block_size : 128;
     c->flags = cfg->flags;
     c->rtl = (cfg->flags & PTGPU_FLAG_ARGS_RTL) ? 1 : 0;
+    c->wide = (cfg->flags & PTGPU_FLAG_BINARY_TRAVERSAL) ? false : true;
     c->w = cfg->width;
     c->h = cfg->height;
     auto bail = [&](int code) { ptgpu_destroy(c); return code; };
@@ -208,7 +212,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_btn, &c->d_btl, &c->d_keys, &c->d_keys_alt, &c->d_keys_tmp, &c->d_vals_alt,
                       &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_block_bounds, &c->d_arrivals,
                       &c->d_tcount, &c->d_tcost,
-                      &c->d_nodes, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
+                      &c->d_nodes, &c->d_nodes4, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
@@ -358,6 +362,13 @@ static int ensure_bvh_buffers(ptgpu_ctx *c) {
     return PTGPU_OK;
 }
 
+static int prepare_wide(ptgpu_ctx *c) {
+    if (c->n_internal <= 0) return PTGPU_OK;
+    CK(c->d_nodes4.ensure((size_t)c->n_internal * 8 * sizeof(float4)));
+    CK(launch_collapse4(c->d_nodes.as<float4>(), c->n_internal, c->d_nodes4.as<float4>(), c->stream));
+    return PTGPU_OK;
+}
+
 static int prepare_bvh_trace(ptgpu_ctx *c) {
     const size_t n = c->n;
     CK(c->d_nodes.ensure((n > 1 ? n - 1 : 1) * 4 * sizeof(float4)));
@@ -371,7 +382,8 @@ static int prepare_bvh_trace(ptgpu_ctx *c) {
     CK(cudaMemcpyAsync(c->d_root_box.p, &root->bound, 6 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     c->root_first = 0;
     c->root_count = n > 1 ? 0 : 1;
-    return PTGPU_OK;
+    c->n_internal = n > 1 ? (int)(n - 1) : 0;
+    return prepare_wide(c);
 }
 
 int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
@@ -450,6 +462,9 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
     CK(cudaMemcpyAsync(c->d_root_box.p, root_box, sizeof(root_box), cudaMemcpyHostToDevice, c->stream));
     CK(launch_gather_prims(c->d_prim_id.as<int32_t>(), (int)nk, c->d_prims0.as<float4>(),
                            c->d_prims.as<float4>(), c->stream));
+    c->n_internal = (int)(nodes.size() / 16);
+    st = prepare_wide(c);
+    if (st) return st;
     CK(cudaStreamSynchronize(c->stream));
     c->last_build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     c->kd_valid = true;

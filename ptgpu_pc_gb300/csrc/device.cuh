@@ -144,6 +144,108 @@ __device__ __forceinline__ bool enter_box(bool hit, float tmin, float tmax, floa
 // (the algorithmic-bytes model of the benchmark).
 struct Counts { uint32_t v, p; };
 
+// ---------------------------------------------------------------------------
+// 4-wide traversal.  Same box test (intersection_bound_test), same culling,
+// nearest child first; leaves are intersected as soon as their box passes.
+// ---------------------------------------------------------------------------
+struct Node4 {
+    float4 q[8];
+};
+
+__device__ __forceinline__ void load_node4(const float4 *nodes4, int idx, Node4 &n) {
+    const float4 *p = nodes4 + 8 * (size_t)idx;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) n.q[k] = __ldg(p + k);
+}
+
+__device__ __forceinline__ float f4get(const float4 &v, int k) {
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ int i4get(const float4 &v, int k) { return __float_as_int(f4get(v, k)); }
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ int traverse4(const TraceView &tv, f3 o, f3 d, float &t, int &prim,
+                                         float maxt, Counts *cnt) {
+    f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    const int skip = tv.n_shapes - 1;
+    int hit_any = 0;
+    float tmin, tmax;
+    if (!slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
+              __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, inv, tmin,
+              tmax))
+        return 0;
+    float tb = ANY ? maxt : t;
+    auto test_range = [&](int first, int count) -> bool {
+        for (int k = first; k < first + count; ++k) {
+            if (ANY && __ldg(&tv.prim_id[k]) == skip) continue;
+            float dd = prim_intersect(tv.prims, k, o, d);
+            if (COUNT) cnt->p++;
+            if (dd != 0.f) {
+                if (ANY) { if (dd < maxt) return true; }
+                else { hit_any = 1; if (dd < tb) { tb = dd; prim = k; } }
+            }
+        }
+        return false;
+    };
+    if (tv.root_count > 0) {
+        bool r = test_range(tv.root_first, tv.root_count);
+        if (!ANY) t = tb;
+        return ANY ? (int)r : hit_any;
+    }
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        Node4 nd;
+        load_node4(tv.nodes4, node, nd);
+        if (COUNT) cnt->v++;
+        int cref[4];
+        float cdist[4];
+        int nc = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int count = i4get(nd.q[7], k);
+            if (count < 0) continue;
+            float t0, t1;
+            bool h = slab(f4get(nd.q[0], k), f4get(nd.q[1], k), f4get(nd.q[2], k),
+                          f4get(nd.q[3], k), f4get(nd.q[4], k), f4get(nd.q[5], k), o, inv, t0, t1);
+            if (!enter_box(h, t0, t1, tb)) continue;
+            const int ref = i4get(nd.q[6], k);
+            if (count > 0) {
+                if (test_range(ref, count)) return 1;
+            } else {
+                cref[nc] = ref;
+                cdist[nc] = t0;
+                ++nc;
+            }
+        }
+        if (nc == 0) {
+            if (sp == 0) break;
+            node = stack[--sp];
+            continue;
+        }
+        // order the internal children nearest first (insertion sort, <= 4)
+#pragma unroll
+        for (int a = 1; a < 4; ++a) {
+            if (a >= nc) break;
+            float dv = cdist[a];
+            int rv = cref[a];
+            int b = a - 1;
+            while (b >= 0 && cdist[b] > dv) { cdist[b + 1] = cdist[b]; cref[b + 1] = cref[b]; --b; }
+            cdist[b + 1] = dv;
+            cref[b + 1] = rv;
+        }
+        for (int a = nc - 1; a >= 1; --a) {
+            if (sp < kStackSize) stack[sp++] = cref[a];
+            else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+        }
+        node = cref[0];
+    }
+    if (!ANY) t = tb;
+    return ANY ? 0 : hit_any;
+}
+
+
 template <bool COUNT = false>
 __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, float &t,
                                              int &prim, int &id, Counts *cnt = nullptr) {
@@ -160,6 +262,11 @@ __device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, fl
         }
         if (prim >= 0) id = prim;
         return t < kInfT;
+    }
+    if (tv.nodes4) {
+        int h = traverse4<false, COUNT>(tv, o, d, t, prim, 0.f, cnt);
+        if (prim >= 0) id = __ldg(&tv.prim_id[prim]);
+        return h;
     }
     f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
     float tmin, tmax;
@@ -244,6 +351,11 @@ __device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float
             if (dd != 0.f && dd < maxt) return true;
         }
         return false;
+    }
+    if (tv.nodes4) {
+        float tt = 0.f;
+        int pp = -1;
+        return traverse4<true, COUNT>(tv, o, d, tt, pp, maxt, cnt) != 0;
     }
     f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
     float tmin, tmax;

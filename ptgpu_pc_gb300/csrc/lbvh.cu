@@ -808,6 +808,57 @@ __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
     }
 }
 
+// Binary traversal nodes -> 4-wide nodes (see types.h): slot k holds a child
+// of binary node i, an internal child being replaced by its two children.
+__global__ void k_collapse4(const float4 *__restrict__ nodes2, int n_int,
+                            float4 *__restrict__ nodes4) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_int) return;
+    float box[4][6];
+    int ref[4], cnt[4];
+    int ns = 0;
+    const float4 *nd = nodes2 + 4 * (size_t)i;
+    float4 q0 = nd[0], q1 = nd[1], q2 = nd[2], q3 = nd[3];
+    const int lref = __float_as_int(q3.x), rref = __float_as_int(q3.y);
+    const int lcnt = __float_as_int(q3.z), rcnt = __float_as_int(q3.w);
+    float lb[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+    float rb[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+    for (int side = 0; side < 2; ++side) {
+        const int r = side ? rref : lref, c = side ? rcnt : lcnt;
+        const float *b = side ? rb : lb;
+        if (c > 0 || r < 0 || r >= n_int) {
+            for (int a = 0; a < 6; ++a) box[ns][a] = b[a];
+            ref[ns] = r; cnt[ns] = c > 0 ? c : -1; ++ns;
+            continue;
+        }
+        const float4 *cn = nodes2 + 4 * (size_t)r;
+        float4 c0 = cn[0], c1 = cn[1], c2 = cn[2], c3 = cn[3];
+        float cl[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
+        float cr[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+        for (int a = 0; a < 6; ++a) box[ns][a] = cl[a];
+        ref[ns] = __float_as_int(c3.x); cnt[ns] = __float_as_int(c3.z); ++ns;
+        for (int a = 0; a < 6; ++a) box[ns][a] = cr[a];
+        ref[ns] = __float_as_int(c3.y); cnt[ns] = __float_as_int(c3.w); ++ns;
+    }
+    for (; ns < 4; ++ns) {
+        box[ns][0] = box[ns][2] = box[ns][4] = 1.f;
+        box[ns][1] = box[ns][3] = box[ns][5] = 0.f;
+        ref[ns] = 0; cnt[ns] = -1;
+    }
+    float4 *o = nodes4 + 8 * (size_t)i;
+    for (int a = 0; a < 6; ++a) o[a] = make_float4(box[0][a], box[1][a], box[2][a], box[3][a]);
+    o[6] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), __int_as_float(ref[2]),
+                       __int_as_float(ref[3]));
+    o[7] = make_float4(__int_as_float(cnt[0]), __int_as_float(cnt[1]), __int_as_float(cnt[2]),
+                       __int_as_float(cnt[3]));
+}
+
+cudaError_t launch_collapse4(const float4 *nodes2, int n_int, float4 *nodes4, cudaStream_t s) {
+    if (n_int <= 0) return cudaSuccess;
+    k_collapse4<<<(n_int + 255) / 256, 256, 0, s>>>(nodes2, n_int, nodes4);
+    return cudaGetLastError();
+}
+
 // gathers prims in a given order (KD-tree kn order)
 __global__ void k_gather_prims(const int32_t *__restrict__ order, int count,
                                const float4 *__restrict__ prims0, float4 *__restrict__ prims) {

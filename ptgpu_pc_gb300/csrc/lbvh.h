@@ -45,6 +45,7 @@ cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int 
 cudaError_t launch_abi_to_trace(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, int n,
                                 const float4 *prims0, float4 *nodes, float4 *prims,
                                 int32_t *prim_id, cudaStream_t s);
+cudaError_t launch_collapse4(const float4 *nodes2, int n_int, float4 *nodes4, cudaStream_t s);
 cudaError_t launch_gather_prims(const int32_t *order, int count, const float4 *prims0,
                                 float4 *prims, cudaStream_t s);
 cudaError_t launch_export_shapes(ptgpu_shape *shapes, const float *verts, const uint8_t *type,

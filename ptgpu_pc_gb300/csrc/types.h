@@ -21,8 +21,16 @@ namespace ptgpu {
 //   triangle: (p1, TRI) (e1, 0) (e2, 0) with e1 = p2-p1, e2 = p3-p1
 //   sphere:   (p, SPH)  (rad*rad, rad, 0, 0) (0)
 // ---------------------------------------------------------------------------
+// 4-wide node (128 B, eight 16-byte loads), one per binary node; a 4-wide
+// node's slots are the binary node's children, an internal child replaced by
+// its own two children.  Traversal starts at node 0 and follows slot refs,
+// so only the nodes at even binary depth are ever visited.
+//   q0..q5 = min_x[4], max_x[4], min_y[4], max_y[4], min_z[4], max_z[4]
+//   q6     = ref[4]   (internal: binary node index; leaf: first prim)
+//   q7     = count[4] (0: internal, > 0: leaf prim count, -1: empty slot)
 struct TraceView {
     const float4 *nodes;     // internal nodes (may be null when the root is a leaf)
+    const float4 *nodes4;    // 4-wide nodes (null: traverse the binary nodes)
     const float4 *prims;     // prims in traversal order
     const int32_t *prim_id;  // traversal-order prim -> shape id
     int32_t accel;           // PTGPU_ACCEL_*
