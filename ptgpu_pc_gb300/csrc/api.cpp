@@ -91,7 +91,7 @@ struct ptgpu_ctx {
     bool kd_valid = false;
     // rendering
     int w = 0, h = 0;
-    DevBuf d_colors, d_pixels, d_seeds, d_err;
+    DevBuf d_colors, d_pixels, d_seeds, d_err, d_pixctr;
     uint32_t *h_pixels = nullptr;
     int current_sample = 0;
     ptgpu_camera cam{};
@@ -192,6 +192,7 @@ int ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out) {
     if ((e = c->d_pixels.ensure(npx * sizeof(uint32_t))) != cudaSuccess) return bail(cuda_fail(e, "alloc pixels"));
     if ((e = c->d_seeds.ensure(npx * 2 * sizeof(uint32_t))) != cudaSuccess) return bail(cuda_fail(e, "alloc seeds"));
     if ((e = c->d_err.ensure(16)) != cudaSuccess) return bail(cuda_fail(e, "alloc error word"));
+    if ((e = c->d_pixctr.ensure(16)) != cudaSuccess) return bail(cuda_fail(e, "alloc pixel counter"));
     if ((e = cudaMallocHost(&c->h_pixels, npx * sizeof(uint32_t))) != cudaSuccess)
         return bail(cuda_fail(e, "alloc pinned pixels"));
     cudaMemsetAsync(c->d_err.p, 0, 16, c->stream);
@@ -213,7 +214,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_block_bounds, &c->d_arrivals,
                       &c->d_tcount, &c->d_tcost,
                       &c->d_nodes, &c->d_nodes4, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
-                      &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_rays, &c->d_t,
+                      &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
     if (c->h_pixels) cudaFreeHost(c->h_pixels);
@@ -584,6 +585,8 @@ static int enqueue_render(ptgpu_ctx *c, uint32_t passes, unsigned long long *sta
     a.pixels = c->d_pixels.as<uint32_t>();
     a.seeds = c->d_seeds.as<uint32_t>();
     a.stats = stats;
+    a.pixel_counter = c->d_pixctr.as<unsigned int>();
+    a.max_ctas = 0;
     CK(launch_render(a, c->block, c->stream));
     c->current_sample += (int)passes;
     return PTGPU_OK;

@@ -138,285 +138,164 @@ __device__ __forceinline__ bool enter_box(bool hit, float tmin, float tmax, floa
     return hit && tmin <= tbest * 1.0001f && tmax >= 0.f;
 }
 
-// Closest hit: returns 1 when any prim reported a non-zero distance (the
-// reference's `intersected`), t/id/prim of the nearest.  Front-to-back order.
-// COUNT: accumulate node visits (v) and primitive tests (p) into cnt[0..1]
-// (the algorithmic-bytes model of the benchmark).
+// ---------------------------------------------------------------------------
+// Ray queries.  One traversal routine serves the closest-hit query
+// (Intersect, rendering_kernel.cl:194-363) and the shadow query (IntersectP,
+// rendering_kernel.cl:375-395: any hit with 0 < d < maxt, the last shape never
+// tested), so a kernel that issues both has a single copy of the loop.
+// Boxes are tested with intersection_bound_test's arithmetic; a box is
+// entered when that test passes and it can still hold a better hit (front to
+// back, nearest child first).  WIDE selects the 4-wide nodes.  COUNT adds
+// node visits (v) and primitive tests (p) to *cnt (the benchmark's
+// bytes-moved model).
+// ---------------------------------------------------------------------------
 struct Counts { uint32_t v, p; };
 
-// ---------------------------------------------------------------------------
-// 4-wide traversal.  Same box test (intersection_bound_test), same culling,
-// nearest child first; leaves are intersected as soon as their box passes.
-// ---------------------------------------------------------------------------
 struct Node4 {
     float4 q[8];
 };
-
-__device__ __forceinline__ void load_node4(const float4 *nodes4, int idx, Node4 &n) {
-    const float4 *p = nodes4 + 8 * (size_t)idx;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) n.q[k] = __ldg(p + k);
-}
 
 __device__ __forceinline__ float f4get(const float4 &v, int k) {
     return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 __device__ __forceinline__ int i4get(const float4 &v, int k) { return __float_as_int(f4get(v, k)); }
 
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ int traverse4(const TraceView &tv, f3 o, f3 d, float &t, int &prim,
-                                         float maxt, Counts *cnt) {
-    f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-    const int skip = tv.n_shapes - 1;
+// returns: closest query -> the reference's `intersected` (t, prim set);
+//          shadow query  -> 1 when occluded
+template <bool WIDE, bool COUNT>
+__device__ __forceinline__ int trace_query(const TraceView &tv, f3 o, f3 d, bool any, float maxt,
+                                           float &t, int &prim, Counts *cnt) {
+    prim = -1;
+    t = kInfT;
+    const int n = tv.n_shapes;
+    if (n <= 0 || (any && n <= 1)) return 0;
+    if (tv.accel == PTGPU_ACCEL_NONE) {
+        if (any) {
+            for (int i = n - 2; i >= 0; --i) {
+                float dd = prim_intersect(tv.prims, i, o, d);
+                if (COUNT) cnt->p++;
+                if (dd != 0.f && dd < maxt) return 1;
+            }
+            return 0;
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            float dd = prim_intersect(tv.prims, i, o, d);
+            if (COUNT) cnt->p++;
+            if (dd != 0.f && dd < t) { t = dd; prim = i; }
+        }
+        return t < kInfT;
+    }
+    const f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    const int skip = n - 1;
+    float tb = any ? maxt : kInfT;
     int hit_any = 0;
     float tmin, tmax;
     if (!slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
               __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, inv, tmin,
               tmax))
         return 0;
-    float tb = ANY ? maxt : t;
-    auto test_range = [&](int first, int count) -> bool {
-        for (int k = first; k < first + count; ++k) {
-            if (ANY && __ldg(&tv.prim_id[k]) == skip) continue;
-            float dd = prim_intersect(tv.prims, k, o, d);
-            if (COUNT) cnt->p++;
-            if (dd != 0.f) {
-                if (ANY) { if (dd < maxt) return true; }
-                else { hit_any = 1; if (dd < tb) { tb = dd; prim = k; } }
-            }
-        }
-        return false;
-    };
-    if (tv.root_count > 0) {
-        bool r = test_range(tv.root_first, tv.root_count);
-        if (!ANY) t = tb;
-        return ANY ? (int)r : hit_any;
-    }
     int stack[kStackSize];
     int sp = 0;
-    int node = 0;
+    // current item: internal node (cnt == 0) or a leaf range (cnt > 0)
+    int cur = tv.root_count > 0 ? tv.root_first : 0;
+    int ccnt = tv.root_count > 0 ? tv.root_count : 0;
     for (;;) {
-        Node4 nd;
-        load_node4(tv.nodes4, node, nd);
-        if (COUNT) cnt->v++;
-        int cref[4];
-        float cdist[4];
-        int nc = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int count = i4get(nd.q[7], k);
-            if (count < 0) continue;
-            float t0, t1;
-            bool h = slab(f4get(nd.q[0], k), f4get(nd.q[1], k), f4get(nd.q[2], k),
-                          f4get(nd.q[3], k), f4get(nd.q[4], k), f4get(nd.q[5], k), o, inv, t0, t1);
-            if (!enter_box(h, t0, t1, tb)) continue;
-            const int ref = i4get(nd.q[6], k);
-            if (count > 0) {
-                if (test_range(ref, count)) return 1;
-            } else {
-                cref[nc] = ref;
-                cdist[nc] = t0;
-                ++nc;
-            }
-        }
-        if (nc == 0) {
-            if (sp == 0) break;
-            node = stack[--sp];
-            continue;
-        }
-        // order the internal children nearest first (insertion sort, <= 4)
-#pragma unroll
-        for (int a = 1; a < 4; ++a) {
-            if (a >= nc) break;
-            float dv = cdist[a];
-            int rv = cref[a];
-            int b = a - 1;
-            while (b >= 0 && cdist[b] > dv) { cdist[b + 1] = cdist[b]; cref[b + 1] = cref[b]; --b; }
-            cdist[b + 1] = dv;
-            cref[b + 1] = rv;
-        }
-        for (int a = nc - 1; a >= 1; --a) {
-            if (sp < kStackSize) stack[sp++] = cref[a];
-            else if (tv.error_flags) atomicOr(tv.error_flags, 1);
-        }
-        node = cref[0];
-    }
-    if (!ANY) t = tb;
-    return ANY ? 0 : hit_any;
-}
-
-
-template <bool COUNT = false>
-__device__ __forceinline__ int trace_closest(const TraceView &tv, f3 o, f3 d, float &t,
-                                             int &prim, int &id, Counts *cnt = nullptr) {
-    t = kInfT;
-    prim = -1;
-    id = 0;
-    int hit_any = 0;
-    if (tv.n_shapes <= 0) return 0;
-    if (tv.accel == PTGPU_ACCEL_NONE) {
-        for (int i = tv.n_shapes - 1; i >= 0; --i) {
-            float dd = prim_intersect(tv.prims, i, o, d);
-            if (COUNT) cnt->p++;
-            if (dd != 0.f && dd < t) { t = dd; prim = i; }
-        }
-        if (prim >= 0) id = prim;
-        return t < kInfT;
-    }
-    if (tv.nodes4) {
-        int h = traverse4<false, COUNT>(tv, o, d, t, prim, 0.f, cnt);
-        if (prim >= 0) id = __ldg(&tv.prim_id[prim]);
-        return h;
-    }
-    f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-    float tmin, tmax;
-    bool rh = slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
-                   __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o,
-                   inv, tmin, tmax);
-    if (!rh) return 0;
-    int stack[kStackSize];
-    int sp = 0;
-    int node_ref, node_cnt;
-    if (tv.root_count > 0) { node_ref = tv.root_first; node_cnt = tv.root_count; }
-    else { node_ref = 0; node_cnt = 0; }
-    // stack entries: internal node index (>= 0) or leaf ~(first | count<<26)?
-    // Leaves are tested as soon as their box passes, so only nodes are pushed.
-    for (;;) {
-        if (node_cnt > 0) {
-            for (int k = node_ref; k < node_ref + node_cnt; ++k) {
+        if (ccnt > 0) {
+            for (int k = cur; k < cur + ccnt; ++k) {
+                if (any && __ldg(&tv.prim_id[k]) == skip) continue;
                 float dd = prim_intersect(tv.prims, k, o, d);
                 if (COUNT) cnt->p++;
                 if (dd != 0.f) {
-                    hit_any = 1;
-                    if (dd < t) { t = dd; prim = k; }
+                    if (any) {
+                        if (dd < maxt) return 1;
+                    } else {
+                        hit_any = 1;
+                        if (dd < tb) { tb = dd; prim = k; }
+                    }
                 }
             }
-        } else {
-            const float4 *nd = tv.nodes + 4 * node_ref;
+        } else if (WIDE) {
+            const float4 *p = tv.nodes4 + 8 * (size_t)cur;
+            Node4 nd;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) nd.q[k] = __ldg(p + k);
             if (COUNT) cnt->v++;
+            // hit children: leaves first in slot order, then internal nodes by distance
+            int iref[4];
+            float idist[4];
+            int ni = 0;
+            int lref[4], lcnt[4];
+            int nl = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int c = i4get(nd.q[7], k);
+                float t0, t1;
+                bool h = slab(f4get(nd.q[0], k), f4get(nd.q[1], k), f4get(nd.q[2], k),
+                              f4get(nd.q[3], k), f4get(nd.q[4], k), f4get(nd.q[5], k), o, inv, t0,
+                              t1);
+                if (c < 0 || !enter_box(h, t0, t1, tb)) continue;
+                if (c > 0) { lref[nl] = i4get(nd.q[6], k); lcnt[nl] = c; ++nl; }
+                else { iref[ni] = i4get(nd.q[6], k); idist[ni] = t0; ++ni; }
+            }
+            // internal children: sort nearest first, push the others far first
+#pragma unroll
+            for (int a = 1; a < 4; ++a) {
+                if (a < ni) {
+                    float dv = idist[a];
+                    int rv = iref[a];
+                    int b = a - 1;
+                    while (b >= 0 && idist[b] > dv) { idist[b + 1] = idist[b]; iref[b + 1] = iref[b]; --b; }
+                    idist[b + 1] = dv;
+                    iref[b + 1] = rv;
+                }
+            }
+            for (int a = ni - 1; a >= 0; --a) {
+                if (sp < kStackSize) stack[sp++] = iref[a];
+                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+            }
+            // leaves go on the stack as negative entries, tested before the nodes
+            for (int a = nl - 1; a >= 0; --a) {
+                if (sp + 1 < kStackSize) { stack[sp++] = lcnt[a]; stack[sp++] = ~lref[a]; }
+                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+            }
+            if (sp == 0) break;
+            int e = stack[--sp];
+            if (e < 0) { cur = ~e; ccnt = stack[--sp]; }
+            else { cur = e; ccnt = 0; }
+            continue;
+        } else {
+            const float4 *nd = tv.nodes + 4 * (size_t)cur;
             float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
             int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+            if (COUNT) cnt->v++;
             float lt0, lt1, rt0, rt1;
             bool lh = slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv, lt0, lt1);
-            bool rhh = slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv, rt0, rt1);
-            lh = enter_box(lh, lt0, lt1, t);
-            rhh = enter_box(rhh, rt0, rt1, t);
-            // leaves are intersected immediately (their box was just tested)
-            if (lh && q3.z > 0) {
-                for (int k = q3.x; k < q3.x + q3.z; ++k) {
-                    float dd = prim_intersect(tv.prims, k, o, d);
-                if (COUNT) cnt->p++;
-                    if (dd != 0.f) { hit_any = 1; if (dd < t) { t = dd; prim = k; } }
-                }
-                lh = false;
-            }
-            if (rhh && q3.w > 0) {
-                for (int k = q3.y; k < q3.y + q3.w; ++k) {
-                    float dd = prim_intersect(tv.prims, k, o, d);
-                if (COUNT) cnt->p++;
-                    if (dd != 0.f) { hit_any = 1; if (dd < t) { t = dd; prim = k; } }
-                }
-                rhh = false;
-            }
-            if (lh && rhh) {
-                int nearc = q3.x, farc = q3.y;
-                if (rt0 < lt0) { nearc = q3.y; farc = q3.x; }
-                if (sp < kStackSize) stack[sp++] = farc;
-                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
-                node_ref = nearc; node_cnt = 0;
+            bool rh = slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv, rt0, rt1);
+            lh = enter_box(lh, lt0, lt1, tb);
+            rh = enter_box(rh, rt0, rt1, tb);
+            if (lh && rh) {
+                // nearer child next, the other onto the stack (leaf: negative pair)
+                bool lfirst = !(rt0 < lt0);
+                int fr = lfirst ? q3.y : q3.x, fc = lfirst ? q3.w : q3.z;
+                int nr = lfirst ? q3.x : q3.y, nc = lfirst ? q3.z : q3.w;
+                if (sp + 1 < kStackSize) {
+                    if (fc > 0) { stack[sp++] = fc; stack[sp++] = ~fr; }
+                    else stack[sp++] = fr;
+                } else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+                cur = nr; ccnt = nc;
                 continue;
             }
-            if (lh) { node_ref = q3.x; node_cnt = 0; continue; }
-            if (rhh) { node_ref = q3.y; node_cnt = 0; continue; }
+            if (lh) { cur = q3.x; ccnt = q3.z; continue; }
+            if (rh) { cur = q3.y; ccnt = q3.w; continue; }
         }
         if (sp == 0) break;
-        node_ref = stack[--sp];
-        node_cnt = 0;
+        int e = stack[--sp];
+        if (e < 0) { cur = ~e; ccnt = stack[--sp]; }
+        else { cur = e; ccnt = 0; }
     }
-    if (prim >= 0) id = __ldg(&tv.prim_id[prim]);
+    if (any) return 0;
+    t = tb;
     return hit_any;
-}
-
-// IntersectP (rendering_kernel.cl:375-395): any hit with 0 < d < maxt among
-// shapes 0..n-2 (the last shape is never tested), accelerated.
-template <bool COUNT = false>
-__device__ __forceinline__ bool trace_any(const TraceView &tv, f3 o, f3 d, float maxt,
-                                          Counts *cnt = nullptr) {
-    const int skip = tv.n_shapes - 1;
-    if (tv.n_shapes <= 1) return false;
-    if (tv.accel == PTGPU_ACCEL_NONE) {
-        for (int i = tv.n_shapes - 2; i >= 0; --i) {
-            float dd = prim_intersect(tv.prims, i, o, d);
-            if (COUNT) cnt->p++;
-            if (dd != 0.f && dd < maxt) return true;
-        }
-        return false;
-    }
-    if (tv.nodes4) {
-        float tt = 0.f;
-        int pp = -1;
-        return traverse4<true, COUNT>(tv, o, d, tt, pp, maxt, cnt) != 0;
-    }
-    f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-    float tmin, tmax;
-    if (!slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
-              __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, inv,
-              tmin, tmax))
-        return false;
-    int stack[kStackSize];
-    int sp = 0;
-    int node_ref = tv.root_count > 0 ? tv.root_first : 0;
-    int node_cnt = tv.root_count > 0 ? tv.root_count : 0;
-    for (;;) {
-        if (node_cnt > 0) {
-            for (int k = node_ref; k < node_ref + node_cnt; ++k) {
-                if (__ldg(&tv.prim_id[k]) == skip) continue;
-                float dd = prim_intersect(tv.prims, k, o, d);
-                if (COUNT) cnt->p++;
-                if (dd != 0.f && dd < maxt) return true;
-            }
-        } else {
-            const float4 *nd = tv.nodes + 4 * node_ref;
-            if (COUNT) cnt->v++;
-            float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
-            int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
-            float lt0, lt1, rt0, rt1;
-            bool lh = enter_box(slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv, lt0, lt1), lt0, lt1, maxt);
-            bool rhh = enter_box(slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv, rt0, rt1), rt0, rt1, maxt);
-            if (lh && q3.z > 0) {
-                for (int k = q3.x; k < q3.x + q3.z; ++k) {
-                    if (__ldg(&tv.prim_id[k]) == skip) continue;
-                    float dd = prim_intersect(tv.prims, k, o, d);
-                if (COUNT) cnt->p++;
-                    if (dd != 0.f && dd < maxt) return true;
-                }
-                lh = false;
-            }
-            if (rhh && q3.w > 0) {
-                for (int k = q3.y; k < q3.y + q3.w; ++k) {
-                    if (__ldg(&tv.prim_id[k]) == skip) continue;
-                    float dd = prim_intersect(tv.prims, k, o, d);
-                if (COUNT) cnt->p++;
-                    if (dd != 0.f && dd < maxt) return true;
-                }
-                rhh = false;
-            }
-            if (lh && rhh) {
-                int nearc = q3.x, farc = q3.y;
-                if (rt0 < lt0) { nearc = q3.y; farc = q3.x; }
-                if (sp < kStackSize) stack[sp++] = farc;
-                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
-                node_ref = nearc; node_cnt = 0;
-                continue;
-            }
-            if (lh) { node_ref = q3.x; node_cnt = 0; continue; }
-            if (rhh) { node_ref = q3.y; node_cnt = 0; continue; }
-        }
-        if (sp == 0) break;
-        node_ref = stack[--sp];
-        node_cnt = 0;
-    }
-    return false;
 }
 
 }  // namespace ptgpu

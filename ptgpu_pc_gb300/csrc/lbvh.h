@@ -68,6 +68,8 @@ struct RenderArgs {
     uint32_t *pixels;           // W*H RGBA8
     uint32_t *seeds;            // 2*W*H
     unsigned long long *stats;  // optional traversal counters (6 words)
+    unsigned int *pixel_counter;// next pixel to hand out (zeroed per launch)
+    int32_t max_ctas;           // grid cap (resident CTAs); 0 = one lane per pixel
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,

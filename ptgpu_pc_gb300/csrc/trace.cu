@@ -1,11 +1,22 @@
 // trace.cu -- closest-hit queries and the per-pixel radiance path tracer.
 //
-// render: one thread per pixel runs all of the frame's passes back to back
-// (RadianceGPU, rendering_kernel.cl:1072-1150, once per pass).  A pixel's
-// passes are sequential by construction -- each pass continues the pixel's
-// seed stream where the previous one left it -- so the pixel is the unit of
-// parallelism; keeping its passes in one thread keeps the seeds, the running
-// mean and the colour in registers for the whole frame and writes them once.
+// The tracer (RadianceGPU, rendering_kernel.cl:1072-1150, with
+// RadiancePathTracing / RadianceOnePathTracing / SampleLights) runs as a
+// per-lane state machine: every iteration of the kernel's loop each lane
+// issues exactly one ray query -- an extension ray or one light's shadow
+// ray -- through a single traversal routine, then consumes its result.
+// Lanes of a warp therefore run the traversal together instead of drifting
+// apart inside nested per-pass / per-bounce / per-light loops.  A lane that
+// has finished all passes of its pixel takes the next pixel from a global
+// counter: the lanes that need work vote (ballot), one atomicAdd reserves a
+// contiguous run, and each lane's slot is its prefix popcount in the vote.
+//
+// A pixel's passes are sequential by construction -- each continues the
+// pixel's seed stream where the previous one stopped -- so one lane runs all
+// of a pixel's passes and keeps its seeds and running mean in registers.
+// Deferring a shadow query to the next loop iteration changes no random
+// draw: SampleLights consumes its two randoms before the visibility test, and
+// the light contributions are summed in light order as in the reference.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -14,228 +25,292 @@
 
 namespace ptgpu {
 
-__global__ void k_trace_closest(TraceView tv, const ptgpu_ray *__restrict__ rays, int n,
-                                float *__restrict__ tout, uint32_t *__restrict__ idout,
-                                int32_t *__restrict__ hitout) {
+template <bool WIDE>
+__global__ void __launch_bounds__(128) k_trace_closest(TraceView tv,
+                                                        const ptgpu_ray *__restrict__ rays, int n,
+                                                        float *__restrict__ tout,
+                                                        uint32_t *__restrict__ idout,
+                                                        int32_t *__restrict__ hitout) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float *rp = reinterpret_cast<const float *>(rays + i);
     f3 o = mk3(rp[0], rp[1], rp[2]);
     f3 d = mk3(rp[3], rp[4], rp[5]);
     float t;
-    int prim, id;
-    int h = trace_closest(tv, o, d, t, prim, id);
+    int prim;
+    int h = trace_query<WIDE, false>(tv, o, d, false, 0.f, t, prim, nullptr);
     tout[i] = t;
-    idout[i] = h ? (uint32_t)id : 0u;
+    idout[i] = (h && prim >= 0) ? (uint32_t)__ldg(&tv.prim_id[prim]) : 0u;
     hitout[i] = h;
-}
-
-// SampleLights (rendering_kernel.cl:397-493) over the emitter list
-template <bool COUNT>
-__device__ __forceinline__ f3 sample_lights(const RenderArgs &a, uint32_t &s0, uint32_t &s1,
-                                            f3 hit, f3 normal, Counts *cnt) {
-    f3 result = mk3(0.f, 0.f, 0.f);
-    for (int li = 0; li < a.n_lights; ++li) {
-        const LightRec L = a.lights[li];
-        f3 lp, ln;
-        float u1, u2;
-        if (a.rtl) { u2 = get_random(s0, s1); u1 = get_random(s0, s1); }
-        else       { u1 = get_random(s0, s1); u2 = get_random(s0, s1); }
-        if (__float_as_int(L.a.w) == PTGPU_TRIANGLE) {
-            float su1 = sqrtf(u1);
-            float bu = 1.0f - su1, bv = u2 * su1;
-            f3 e1 = smul3(bu, mk3(L.b.x, L.b.y, L.b.z));
-            f3 e2 = smul3(bv, mk3(L.c.x, L.c.y, L.c.z));
-            lp = add3(add3(mk3(L.a.x, L.a.y, L.a.z), e1), e2);
-            ln = norm3(cross3(e1, e2));
-        } else {
-            const float zz = 1.f - 2.f * u1;
-            const float rr = sqrtf(fmaxf(0.f, 1.f - zz * zz));
-            const float phi = 2.f * kPi * u2;
-            float sphi, cphi;
-            pt_sincos(phi, sphi, cphi);
-            f3 unit = mk3(rr * cphi, rr * sphi, zz);
-            lp = add3(smul3(L.b.x, unit), mk3(L.a.x, L.a.y, L.a.z));
-            ln = unit;
-        }
-        f3 sd = sub3(lp, hit);
-        const float len = sqrtf(dot3(sd, sd));
-        sd = smul3(1.f / len, sd);
-        float wo = dot3(sd, ln);
-        if (wo > 0.f) continue;
-        wo = -wo;
-        wo = cl_clamp(wo, 0.f, 1.f);
-        const float wi = dot3(sd, normal);
-        if (COUNT && wi > 0.f) cnt[2].v++;   // shadow query issued
-        if (wi > 0.f && !trace_any<COUNT>(a.tv, hit, sd, len - kEps, cnt + 1)) {
-            const float s = L.b.w * wi * wo / (len * len);
-            result = add3(result, smul3(s, mk3(L.e.x, L.e.y, L.e.z)));
-        }
-    }
-    return result;
-}
-
-// RadiancePathTracing + RadianceOnePathTracing (rendering_kernel.cl:495-820)
-template <bool COUNT>
-__device__ __forceinline__ f3 radiance(const RenderArgs &a, f3 o, f3 d, uint32_t &s0,
-                                       uint32_t &s1, Counts *cnt) {
-    f3 rad = mk3(0.f, 0.f, 0.f);
-    f3 tp = mk3(1.f, 1.f, 1.f);
-    int specular = 1;
-    for (int depth = 0; depth <= a.max_depth; ++depth) {
-        float t;
-        int prim, id;
-        if (COUNT) cnt[2].p++;   // extension query issued
-        if (!trace_closest<COUNT>(a.tv, o, d, t, prim, id, cnt)) break;
-        f3 hp = add3(o, smul3(t, d));
-        const Material m = a.mats[id];
-        const int type = __float_as_int(m.e_type.w);
-        f3 normal;
-        {
-            // geometry of the hit from the traversal-order prims; a hit
-            // reported only beyond t = 1e20 keeps the reference's id = 0
-            const int k = prim >= 0 ? prim : 0;
-            const float4 *pp = prim >= 0 ? a.tv.prims : a.prims0;
-            float4 g0 = __ldg(&pp[3 * k + 0]);
-            if (type == PTGPU_SPHERE) {
-                normal = sub3(hp, mk3(g0.x, g0.y, g0.z));
-            } else {
-                float4 g1 = __ldg(&pp[3 * k + 1]);
-                float4 g2 = __ldg(&pp[3 * k + 2]);
-                normal = cross3(mk3(g1.x, g1.y, g1.z), mk3(g2.x, g2.y, g2.z));
-            }
-        }
-        normal = norm3(normal);
-        const float dp = dot3(normal, d);
-        const float inv_sign = -1.f * cl_sign(dp);
-        f3 nl = smul3(inv_sign, normal);
-        f3 ecol = mk3(m.e_type.x, m.e_type.y, m.e_type.z);
-        if (!iszero3(ecol)) {
-            if (specular) {
-                ecol = smul3(fabsf(dp), ecol);
-                ecol = mul3(tp, ecol);
-                rad = add3(rad, ecol);
-            }
-            break;
-        }
-        f3 col = mk3(m.c_refl.x, m.c_refl.y, m.c_refl.z);
-        const int refl = __float_as_int(m.c_refl.w);
-        if (refl == PTGPU_DIFF) {
-            specular = 0;
-            tp = mul3(tp, col);
-            f3 ld = sample_lights<COUNT>(a, s0, s1, hp, nl, cnt);
-            ld = mul3(ld, tp);
-            rad = add3(rad, ld);
-            float r1 = 2.f * kPi * get_random(s0, s1);
-            float r2 = get_random(s0, s1);
-            float r2s = sqrtf(r2);
-            f3 w = nl;
-            f3 av = (fabsf(w.x) > .1f) ? mk3(0.f, 1.f, 0.f) : mk3(1.f, 0.f, 0.f);
-            f3 u = norm3(cross3(av, w));
-            f3 v = cross3(w, u);
-            float sr1, cr1;
-            pt_sincos(r1, sr1, cr1);
-            u = smul3(cr1 * r2s, u);
-            v = smul3(sr1 * r2s, v);
-            f3 nd = add3(u, v);
-            w = smul3(sqrtf(1.f - r2), w);
-            nd = add3(nd, w);
-            o = hp; d = nd;
-        } else if (refl == PTGPU_SPEC) {
-            specular = 1;
-            f3 nd = sub3(d, smul3(2.f * dot3(normal, d), normal));
-            tp = mul3(tp, col);
-            o = hp; d = nd;
-        } else {
-            specular = 1;
-            f3 refl_d = sub3(d, smul3(2.f * dot3(normal, d), normal));
-            const bool into = dot3(normal, nl) > 0;
-            const float nc = 1.f, nt = 1.5f;
-            const float nnt = into ? nc / nt : nt / nc;
-            const float ddn = dot3(d, nl);
-            const float cos2t = 1.f - nnt * nnt * (1.f - ddn * ddn);
-            if (cos2t < 0.f) {
-                tp = mul3(tp, col);
-                o = hp; d = refl_d;
-                continue;
-            }
-            const float kk = (float)(into ? 1 : -1) * (ddn * nnt + sqrtf(cos2t));
-            f3 nkk = smul3(kk, normal);
-            f3 tdir = norm3(sub3(smul3(nnt, d), nkk));
-            const float aa = nt - nc, bb = nt + nc;
-            const float R0 = aa * aa / (bb * bb);
-            const float c = 1.f - (into ? -ddn : dot3(tdir, normal));
-            const float Re = R0 + (1.f - R0) * c * c * c * c * c;
-            const float Tr = 1.f - Re;
-            const float P = .25f + .5f * Re;
-            const float RP = Re / P;
-            const float TP = Tr / (1.f - P);
-            if (get_random(s0, s1) < P) {
-                tp = smul3(RP, tp);
-                tp = mul3(tp, col);
-                o = hp; d = refl_d;
-            } else {
-                tp = smul3(TP, tp);
-                tp = mul3(tp, col);
-                o = hp; d = tdir;
-            }
-        }
-    }
-    return rad;
 }
 
 __device__ __forceinline__ uint32_t to_int(float x) {
     return (uint32_t)(int)(powf(cl_clamp(x, 0.f, 1.f), 1.f / 2.2f) * 255.f + .5f);
 }
 
-// COUNT = true: the same kernel, also accumulating into a.stats[6]: extension
-// node visits, prim tests; shadow node visits, prim tests; extension and
-// shadow query counts.
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_render(const RenderArgs a) {
+enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
+
+template <bool WIDE, bool COUNT>
+__global__ void __launch_bounds__(128) k_render(const RenderArgs a, unsigned int *pixel_counter) {
+    const int npx = a.width * a.height;
+    const int lane = threadIdx.x & 31;
+    const float inv_w = 1.f / (float)a.width, inv_h = 1.f / (float)a.height;
+    int state = ST_NEED;
+    int gid = 0, passes_done = 0, depth = 0, li = 0, specular = 1;
+    uint32_t s0 = 0, s1 = 0;
+    f3 col = mk3(0.f, 0.f, 0.f), o = col, d = col, rad = col, tp = col, hp = col, nl = col;
+    f3 ld = col, pend = col;
+    f3 qo = col, qd = col;
+    float qmax = 0.f;
+    bool qany = false;
     Counts cnt[3] = {{0, 0}, {0, 0}, {0, 0}};
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int w = a.width, h = a.height;
-    if (gid >= w * h) return;
-    const int x = gid % w, y = gid / w;
-    uint2 sd = reinterpret_cast<const uint2 *>(a.seeds)[gid];
-    uint32_t s0 = sd.x, s1 = sd.y;
-    const int ci = (h - y - 1) * w + x;
-    f3 col = mk3(0.f, 0.f, 0.f);
-    if (a.start_sample > 0) {
-        const ptgpu_vec c = a.colors[ci];
-        col = mk3(c.x, c.y, c.z);
-    }
-    const float inv_w = 1.f / (float)w, inv_h = 1.f / (float)h;
-    const ptgpu_camera &cam = a.cam;
-    for (int p = 0; p < a.passes; ++p) {
-        const int cs = a.start_sample + p;
-        // GenerateCameraRay (rendering_kernel.cl:1042-1070)
-        const float r1 = get_random(s0, s1) - .5f;
-        const float r2 = get_random(s0, s1) - .5f;
-        const float kcx = ((float)x + r1) * inv_w - .5f;
-        const float kcy = ((float)y + r2) * inv_h - .5f;
-        f3 rdir = mk3(cam.x.x * kcx + cam.y.x * kcy + cam.dir.x,
-                      cam.x.y * kcx + cam.y.y * kcy + cam.dir.y,
-                      cam.x.z * kcx + cam.y.z * kcy + cam.dir.z);
-        f3 rorig = add3(smul3(0.1f, rdir), mk3(cam.orig.x, cam.orig.y, cam.orig.z));
-        rdir = norm3(rdir);
-        f3 r = radiance<COUNT>(a, rorig, rdir, s0, s1, cnt);
-        if (cs == 0) {
-            col = r;
-        } else {
-            const float k1 = (float)cs;
-            const float k2 = 1.f / ((float)cs + 1.f);
-            col.x = (col.x * k1 + r.x) * k2;
-            col.y = (col.y * k1 + r.y) * k2;
-            col.z = (col.z * k1 + r.z) * k2;
+
+    for (;;) {
+        // ---- refill lanes that finished their pixel
+        const bool need = state == ST_NEED;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        if (nm) {
+            const int leader = __ffs(nm) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(pixel_counter, (unsigned)__popc(nm));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                gid = (int)(base + __popc(nm & ((1u << lane) - 1u)));
+                if (gid >= npx) {
+                    state = ST_DONE;
+                } else {
+                    const uint2 sd = reinterpret_cast<const uint2 *>(a.seeds)[gid];
+                    s0 = sd.x; s1 = sd.y;
+                    if (a.start_sample > 0) {
+                        const int x = gid % a.width, y = gid / a.width;
+                        const ptgpu_vec c = a.colors[(a.height - y - 1) * a.width + x];
+                        col = mk3(c.x, c.y, c.z);
+                    }
+                    passes_done = 0;
+                    state = ST_GEN;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, state == ST_DONE)) break;
+
+        // ---- produce this lane's query
+        bool has_q = false;
+        if (state == ST_GEN) {
+            // GenerateCameraRay (rendering_kernel.cl:1042-1070)
+            const int x = gid % a.width, y = gid / a.width;
+            const ptgpu_camera &cam = a.cam;
+            const float r1 = get_random(s0, s1) - .5f;
+            const float r2 = get_random(s0, s1) - .5f;
+            const float kcx = ((float)x + r1) * inv_w - .5f;
+            const float kcy = ((float)y + r2) * inv_h - .5f;
+            f3 rdir = mk3(cam.x.x * kcx + cam.y.x * kcy + cam.dir.x,
+                          cam.x.y * kcx + cam.y.y * kcy + cam.dir.y,
+                          cam.x.z * kcx + cam.y.z * kcy + cam.dir.z);
+            o = add3(smul3(0.1f, rdir), mk3(cam.orig.x, cam.orig.y, cam.orig.z));
+            d = norm3(rdir);
+            rad = mk3(0.f, 0.f, 0.f);
+            tp = mk3(1.f, 1.f, 1.f);
+            specular = 1;
+            depth = 0;
+            state = ST_EXT;
+        }
+        if (state == ST_NEE) {
+            // SampleLights (rendering_kernel.cl:397-493): the next light that
+            // needs a visibility test
+            while (li < a.n_lights) {
+                const LightRec L = a.lights[li];
+                float u1, u2;
+                if (a.rtl) { u2 = get_random(s0, s1); u1 = get_random(s0, s1); }
+                else       { u1 = get_random(s0, s1); u2 = get_random(s0, s1); }
+                f3 lp, lnrm;
+                if (__float_as_int(L.a.w) == PTGPU_TRIANGLE) {
+                    const float su1 = sqrtf(u1);
+                    const float bu = 1.0f - su1, bv = u2 * su1;
+                    const f3 e1 = smul3(bu, mk3(L.b.x, L.b.y, L.b.z));
+                    const f3 e2 = smul3(bv, mk3(L.c.x, L.c.y, L.c.z));
+                    lp = add3(add3(mk3(L.a.x, L.a.y, L.a.z), e1), e2);
+                    lnrm = norm3(cross3(e1, e2));
+                } else {
+                    const float zz = 1.f - 2.f * u1;
+                    const float rr = sqrtf(fmaxf(0.f, 1.f - zz * zz));
+                    const float phi = 2.f * kPi * u2;
+                    float sphi, cphi;
+                    pt_sincos(phi, sphi, cphi);
+                    const f3 unit = mk3(rr * cphi, rr * sphi, zz);
+                    lp = add3(smul3(L.b.x, unit), mk3(L.a.x, L.a.y, L.a.z));
+                    lnrm = unit;
+                }
+                f3 sd = sub3(lp, hp);
+                const float len = sqrtf(dot3(sd, sd));
+                sd = smul3(1.f / len, sd);
+                float wo = dot3(sd, lnrm);
+                if (wo > 0.f) { ++li; continue; }
+                wo = -wo;
+                wo = cl_clamp(wo, 0.f, 1.f);
+                const float wi = dot3(sd, nl);
+                if (wi > 0.f) {
+                    const float s = L.b.w * wi * wo / (len * len);
+                    pend = smul3(s, mk3(L.e.x, L.e.y, L.e.z));
+                    qo = hp; qd = sd; qmax = len - kEps; qany = true;
+                    has_q = true;
+                    if (COUNT) cnt[2].v++;
+                    break;
+                }
+                ++li;
+            }
+            if (!has_q) {
+                // all lights done: Ld * throughput, then the diffuse bounce
+                ld = mul3(ld, tp);
+                rad = add3(rad, ld);
+                const float r1 = 2.f * kPi * get_random(s0, s1);
+                const float r2 = get_random(s0, s1);
+                const float r2s = sqrtf(r2);
+                f3 w = nl;
+                const f3 av = (fabsf(w.x) > .1f) ? mk3(0.f, 1.f, 0.f) : mk3(1.f, 0.f, 0.f);
+                f3 u = norm3(cross3(av, w));
+                f3 v = cross3(w, u);
+                float sr1, cr1;
+                pt_sincos(r1, sr1, cr1);
+                u = smul3(cr1 * r2s, u);
+                v = smul3(sr1 * r2s, v);
+                f3 nd = add3(u, v);
+                w = smul3(sqrtf(1.f - r2), w);
+                nd = add3(nd, w);
+                o = hp;
+                d = nd;
+                state = ++depth > a.max_depth ? -1 : ST_EXT;   // -1: pass finished
+            }
+        }
+        if (state == ST_EXT) {
+            qo = o; qd = d; qany = false; has_q = true;
+            if (COUNT) cnt[2].p++;
+        }
+
+        // ---- the query
+        float t = 0.f;
+        int prim = -1;
+        int hit = 0;
+        if (has_q)
+            hit = trace_query<WIDE, COUNT>(a.tv, qo, qd, qany, qmax, t, prim, cnt + (qany ? 1 : 0));
+
+        // ---- consume it
+        if (has_q && qany) {
+            if (!hit) ld = add3(ld, pend);
+            ++li;
+        } else if (has_q) {
+            // RadianceOnePathTracing (rendering_kernel.cl:495-753)
+            if (!hit) {
+                state = -1;
+            } else {
+                hp = add3(o, smul3(t, d));
+                const int id = prim >= 0 ? __ldg(&a.tv.prim_id[prim]) : 0;
+                const Material m = a.mats[id];
+                const int type = __float_as_int(m.e_type.w);
+                const float4 *pp = prim >= 0 ? a.tv.prims : a.prims0;
+                const int k = prim >= 0 ? prim : 0;
+                const float4 g0 = __ldg(&pp[3 * k + 0]);
+                f3 normal;
+                if (type == PTGPU_SPHERE) {
+                    normal = sub3(hp, mk3(g0.x, g0.y, g0.z));
+                } else {
+                    const float4 g1 = __ldg(&pp[3 * k + 1]);
+                    const float4 g2 = __ldg(&pp[3 * k + 2]);
+                    normal = cross3(mk3(g1.x, g1.y, g1.z), mk3(g2.x, g2.y, g2.z));
+                }
+                normal = norm3(normal);
+                const float dp = dot3(normal, d);
+                const float inv_sign = -1.f * cl_sign(dp);
+                nl = smul3(inv_sign, normal);
+                f3 ecol = mk3(m.e_type.x, m.e_type.y, m.e_type.z);
+                const f3 colr = mk3(m.c_refl.x, m.c_refl.y, m.c_refl.z);
+                const int refl = __float_as_int(m.c_refl.w);
+                if (!iszero3(ecol)) {
+                    if (specular) {
+                        ecol = smul3(fabsf(dp), ecol);
+                        ecol = mul3(tp, ecol);
+                        rad = add3(rad, ecol);
+                    }
+                    state = -1;
+                } else if (refl == PTGPU_DIFF) {
+                    specular = 0;
+                    tp = mul3(tp, colr);
+                    ld = mk3(0.f, 0.f, 0.f);
+                    li = 0;
+                    state = ST_NEE;
+                } else if (refl == PTGPU_SPEC) {
+                    specular = 1;
+                    const f3 ndir = sub3(d, smul3(2.f * dot3(normal, d), normal));
+                    tp = mul3(tp, colr);
+                    o = hp;
+                    d = ndir;
+                    state = ++depth > a.max_depth ? -1 : ST_EXT;
+                } else {
+                    specular = 1;
+                    const f3 refl_d = sub3(d, smul3(2.f * dot3(normal, d), normal));
+                    const bool into = dot3(normal, nl) > 0;
+                    const float nc = 1.f, nt = 1.5f;
+                    const float nnt = into ? nc / nt : nt / nc;
+                    const float ddn = dot3(d, nl);
+                    const float cos2t = 1.f - nnt * nnt * (1.f - ddn * ddn);
+                    if (cos2t < 0.f) {
+                        tp = mul3(tp, colr);
+                        o = hp;
+                        d = refl_d;
+                    } else {
+                        const float kk = (float)(into ? 1 : -1) * (ddn * nnt + sqrtf(cos2t));
+                        const f3 nkk = smul3(kk, normal);
+                        const f3 tdir = norm3(sub3(smul3(nnt, d), nkk));
+                        const float aa = nt - nc, bb = nt + nc;
+                        const float R0 = aa * aa / (bb * bb);
+                        const float c = 1.f - (into ? -ddn : dot3(tdir, normal));
+                        const float Re = R0 + (1.f - R0) * c * c * c * c * c;
+                        const float Tr = 1.f - Re;
+                        const float P = .25f + .5f * Re;
+                        const float RP = Re / P;
+                        const float TP = Tr / (1.f - P);
+                        if (get_random(s0, s1) < P) {
+                            tp = smul3(RP, tp);
+                            tp = mul3(tp, colr);
+                            o = hp;
+                            d = refl_d;
+                        } else {
+                            tp = smul3(TP, tp);
+                            tp = mul3(tp, colr);
+                            o = hp;
+                            d = tdir;
+                        }
+                    }
+                    state = ++depth > a.max_depth ? -1 : ST_EXT;
+                }
+            }
+        }
+
+        // ---- a finished pass: running mean, next pass or next pixel
+        if (state == -1) {
+            const int cs = a.start_sample + passes_done;
+            if (cs == 0) {
+                col = rad;
+            } else {
+                const float k1 = (float)cs;
+                const float k2 = 1.f / ((float)cs + 1.f);
+                col.x = (col.x * k1 + rad.x) * k2;
+                col.y = (col.y * k1 + rad.y) * k2;
+                col.z = (col.z * k1 + rad.z) * k2;
+            }
+            if (++passes_done < a.passes) {
+                state = ST_GEN;
+            } else {
+                const int x = gid % a.width, y = gid / a.width;
+                ptgpu_vec out;
+                out.x = col.x; out.y = col.y; out.z = col.z;
+                a.colors[(a.height - y - 1) * a.width + x] = out;
+                a.pixels[gid] = to_int(col.x) | (to_int(col.y) << 8) | (to_int(col.z) << 16) |
+                                0xff000000u;
+                reinterpret_cast<uint2 *>(a.seeds)[gid] = make_uint2(s0, s1);
+                state = ST_NEED;
+            }
         }
     }
-    ptgpu_vec out;
-    out.x = col.x; out.y = col.y; out.z = col.z;
-    a.colors[ci] = out;
-    a.pixels[gid] = to_int(col.x) | (to_int(col.y) << 8) | (to_int(col.z) << 16) | 0xff000000u;
-    reinterpret_cast<uint2 *>(a.seeds)[gid] = make_uint2(s0, s1);
     if (COUNT) {
         atomicAdd(a.stats + 0, (unsigned long long)cnt[0].v);
         atomicAdd(a.stats + 1, (unsigned long long)cnt[0].p);
@@ -250,15 +325,35 @@ cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {
     const int n = a.width * a.height;
     if (n <= 0 || a.passes <= 0) return cudaSuccess;
     if (block <= 0) block = 128;
-    if (a.stats) k_render<true><<<(n + block - 1) / block, block, 0, s>>>(a);
-    else k_render<false><<<(n + block - 1) / block, block, 0, s>>>(a);
+    if (!a.pixel_counter) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(a.pixel_counter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    // lanes pull pixels until none remain; max_ctas caps the grid at what is resident
+    const bool wide = a.tv.nodes4 != nullptr;
+    int grid = (n + block - 1) / block;
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (wide) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render<true, false>, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render<false, false>, block, 0);
+    int resident = per_sm * sms;
+    if (a.max_ctas > 0 && resident > a.max_ctas) resident = a.max_ctas;
+    if (resident > 0 && grid > resident) grid = resident;
+    if (a.stats) {
+        if (wide) k_render<true, true><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else k_render<false, true><<<grid, block, 0, s>>>(a, a.pixel_counter);
+    } else {
+        if (wide) k_render<true, false><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else k_render<false, false><<<grid, block, 0, s>>>(a, a.pixel_counter);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
                                  uint32_t *id, int32_t *hit, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_trace_closest<<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
+    if (tv.nodes4) k_trace_closest<true><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
+    else k_trace_closest<false><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
     return cudaGetLastError();
 }
 

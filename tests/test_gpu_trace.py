@@ -100,3 +100,21 @@ def test_closest_spheres_bruteforce(built_lib, orc):
         assert (g[2] == o[2]).all()
         assert (g[1][g[2] == 1] == o[1][o[2] == 1]).all()
         assert np.array_equal(g[0].view(np.uint32), o[0].view(np.uint32))
+
+
+@pytest.mark.parametrize("accel", [abi.ACCEL_BVH, abi.ACCEL_KDTREE])
+def test_binary_and_wide_traversal_agree(accel, built_lib, orc):
+    """The 2-wide and the 4-wide node layouts give the same closest hits."""
+    import ptgpu_pc_gb300 as pt
+    shapes, lc, cam = scenes.icosphere_scene(level=5)
+    rays = scenes.random_rays(20_000, seed=16)
+    rays["o"] = rays["o"] * np.float32(40.0) + np.array([30, 20, 60], np.float32)
+    out = []
+    for flags in (0, abi.FLAG_BINARY_TRAVERSAL):
+        with pt.Context(8, 8, flags=flags) as ctx:
+            ctx.set_shapes(shapes, lc)
+            ctx.build(accel)
+            out.append(ctx.trace_closest(rays))
+    assert np.array_equal(out[0][2], out[1][2])
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert (out[0][1] == out[1][1]).mean() > 0.9999
