@@ -91,7 +91,7 @@ struct ptgpu_ctx {
     bool kd_valid = false;
     // rendering
     int w = 0, h = 0;
-    DevBuf d_colors, d_pixels, d_seeds, d_err, d_pixctr;
+    DevBuf d_colors, d_pixels, d_seeds, d_err, d_pixctr, d_wf;
     uint32_t *h_pixels = nullptr;
     int current_sample = 0;
     ptgpu_camera cam{};
@@ -214,7 +214,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_block_bounds, &c->d_arrivals,
                       &c->d_tcount, &c->d_tcost,
                       &c->d_nodes, &c->d_nodes4, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
-                      &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_rays, &c->d_t,
+                      &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_wf, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
     if (c->h_pixels) cudaFreeHost(c->h_pixels);
@@ -587,7 +587,22 @@ static int enqueue_render(ptgpu_ctx *c, uint32_t passes, unsigned long long *sta
     a.stats = stats;
     a.pixel_counter = c->d_pixctr.as<unsigned int>();
     a.max_ctas = 0;
-    CK(launch_render(a, c->block, c->stream));
+    if (!stats && (c->flags & PTGPU_FLAG_WAVEFRONT) && c->n_lights <= kWfMaxLights) {
+        // path slots: all pixels at once unless that needs more than 2 GB
+        const int npx = c->w * c->h;
+        int paths = npx;
+        while (paths > 4096 && wf_carve_bytes(paths, c->n_lights) > (size_t(2) << 30)) paths = (paths + 1) / 2;
+        CK(c->d_wf.ensure(wf_carve_bytes(paths, c->n_lights)));
+        WfArgs w;
+        std::memset(&w, 0, sizeof(w));
+        w.r = a;
+        w.paths = paths;
+        wf_carve(w, c->d_wf.p, paths, c->n_lights);
+        const int grid = c->sm_count * 12;
+        CK(launch_wavefront(w, (int)passes * (c->max_depth + 1), grid, c->stream));
+    } else {
+        CK(launch_render(a, c->block, c->stream));
+    }
     c->current_sample += (int)passes;
     return PTGPU_OK;
 }

@@ -72,6 +72,26 @@ struct RenderArgs {
     int32_t max_ctas;           // grid cap (resident CTAs); 0 = one lane per pixel
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
+
+// wavefront.cu: path state for `paths` slots (struct of arrays, carved from
+// one allocation of wf_carve_bytes) and the queues between the kernels
+struct WfArgs {
+    RenderArgs r;
+    int32_t paths;
+    float4 *o, *d, *rad, *tp, *col;
+    uint2 *seeds;
+    int4 *meta;                 // (depth, specularBounce, passes done, pixel)
+    int2 *nee;                  // (first shadow entry, count)
+    float2 *hit;                // (t, prim as int bits; -2 = miss)
+    int *ext_in, *ext_out, *pend;
+    float4 *sh_o, *sh_d, *sh_c; // shadow ray origin+maxt, dir+path, contribution
+    unsigned char *sh_vis;
+    unsigned *counters;         // ext in, ext out, shadow, pending
+};
+constexpr int kWfMaxLights = 8;
+size_t wf_carve_bytes(int paths, int n_lights);
+void wf_carve(WfArgs &a, void *base, int paths, int n_lights);
+cudaError_t launch_wavefront(WfArgs a, int iterations, int grid, cudaStream_t s);
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
                                  uint32_t *id, int32_t *hit, cudaStream_t s);
 

@@ -132,3 +132,30 @@ def test_mean_luminance_within_3_sigma(built_lib, orc):
     seeds = orc.make_seeds(100, 2 * w * h)
     g_col, _, _ = _gpu_render(shapes, lc, cam, w, h, seeds, 2, abi.ACCEL_BVH)
     assert abs(g_col.view(np.float32).mean() - means[0]) <= 3 * sigma
+
+
+@pytest.mark.parametrize("accel", [abi.ACCEL_NONE, abi.ACCEL_BVH, abi.ACCEL_KDTREE])
+def test_wavefront_matches_lane_tracer(accel, built_lib, orc):
+    """The wavefront kernels and the per-lane tracer compute the same image,
+    bit for bit, including progressive calls that continue the running mean."""
+    shapes, lc, cam = scenes.icosphere_scene(level=3)
+    if accel == abi.ACCEL_NONE:
+        shapes, lc, cam = scenes.cornell_spheres()
+    w, h = 40, 36
+    seeds = orc.make_seeds(6, 2 * w * h)
+    a = _gpu_render(shapes, lc, cam, w, h, seeds, 3, accel, max_depth=7, chunks=[2, 1])
+    b = _gpu_render(shapes, lc, cam, w, h, seeds, 3, accel, max_depth=7, chunks=[2, 1],
+                    flags=abi.FLAG_WAVEFRONT)
+    assert a[0].tobytes() == b[0].tobytes()
+    assert (a[1] == b[1]).all() and (a[2] == b[2]).all()
+
+
+def test_wavefront_vs_oracle(built_lib, orc):
+    shapes, lc, cam = scenes.icosphere_scene(level=4)
+    w = h = 48
+    seeds = orc.make_seeds(7, 2 * w * h)
+    g_col, _, g_sd = _gpu_render(shapes, lc, cam, w, h, seeds, 2, abi.ACCEL_BVH, max_depth=8,
+                                 flags=abi.FLAG_WAVEFRONT)
+    o_col, _, o_sd = _oracle_render(shapes, lc, cam, w, h, seeds, 2, abi.ACCEL_BVH, orc, max_depth=8)
+    assert _rel_rmse(g_col, o_col) < RMSE_TOL
+    assert (g_sd == o_sd).mean() > 0.99
