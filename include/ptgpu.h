@@ -115,8 +115,8 @@ typedef struct {
 #define PTGPU_FLAG_WAVEFRONT     0x1  /* render with the queue-based wavefront  */
 #define PTGPU_FLAG_MORTON_DELTA  0x2  /* Karras split on Morton keys (quality)  */
 #define PTGPU_FLAG_TREELET       0x4  /* treelet reoptimisation after refit     */
-#define PTGPU_FLAG_BINARY_TRAVERSAL 0x10 /* traverse the 2-wide nodes (default:
-                                         4-wide nodes collapsed from them)      */
+#define PTGPU_FLAG_WIDE_TRAVERSAL 0x10 /* traverse 4-wide nodes collapsed from
+                                         the 2-wide ones (default: 2-wide)      */
 #define PTGPU_FLAG_ARGS_RTL      0x8  /* draw the two randoms of a light sample
                                          right-to-left (the order g++ gives the
                                          reference source; the default is the

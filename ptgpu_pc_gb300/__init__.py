@@ -13,7 +13,7 @@ import numpy as np
 from . import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libptgpu.so")
+LIB_PATH = os.environ.get("PTGPU_LIB", os.path.join(HERE, "libptgpu.so"))
 
 # every entry point declared in include/ptgpu.h
 EXPORTS = [

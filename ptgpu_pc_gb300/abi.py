@@ -63,7 +63,7 @@ FLAG_WAVEFRONT = 0x1
 FLAG_MORTON_DELTA = 0x2
 FLAG_TREELET = 0x4
 FLAG_ARGS_RTL = 0x8
-FLAG_BINARY_TRAVERSAL = 0x10
+FLAG_WIDE_TRAVERSAL = 0x10
 
 
 def triangles(p1, p2, p3, e=(0.0, 0.0, 0.0), c=(0.75, 0.75, 0.75), refl=DIFF):

@@ -41,22 +41,26 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False):
+def build(force=False, verbose=False, out_dir=None, lib_path=None, extra_nvcc=()):
+    """Compiles into out_dir (default _build/) and links lib_path (default
+    libptgpu.so); extra_nvcc adds nvcc flags (tuning experiments)."""
+    out_dir = out_dir or OUT_DIR
+    lib_path = lib_path or LIB
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(out_dir, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "ptgpu.h")]
     jobs = []
     objs = []
     for s in CU_SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT_DIR, s + ".o")
+        obj = os.path.join(out_dir, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc] + NVCC_FLAGS + list(extra_nvcc) + ["-c", src, "-o", obj])
     for s in CPP_SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT_DIR, s + ".o")
+        obj = os.path.join(out_dir, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             jobs.append(["g++"] + CXX_FLAGS + ["-I", os.path.join(cuda, "include"), "-c", src, "-o", obj])
@@ -71,15 +75,15 @@ def build(force=False, verbose=False):
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError("compile failed: %s" % cmd[-3])
-    if force or jobs or not os.path.exists(LIB):
-        tmp = LIB + ".tmp"
+    if force or jobs or not os.path.exists(lib_path):
+        tmp = lib_path + ".tmp"
         cmd = [nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lrt", "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link failed")
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

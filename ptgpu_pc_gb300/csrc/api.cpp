@@ -85,7 +85,7 @@ struct ptgpu_ctx {
     DevBuf d_status, d_state, d_block_bounds, d_arrivals, d_tcount, d_tcost;
     DevBuf d_nodes, d_nodes4, d_prims, d_prim_id, d_root_box, d_identity;
     int n_internal = 0;
-    bool wide = true;
+    bool wide = false;
     int32_t root_first = 0, root_count = 0;
     KdTree kd;
     bool kd_valid = false;
@@ -171,7 +171,7 @@ int ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out) {
     c->block = cfg->block_size > 0 ? cfg->block_size : 128;
     c->flags = cfg->flags;
     c->rtl = (cfg->flags & PTGPU_FLAG_ARGS_RTL) ? 1 : 0;
-    c->wide = (cfg->flags & PTGPU_FLAG_BINARY_TRAVERSAL) ? false : true;
+    c->wide = (cfg->flags & PTGPU_FLAG_WIDE_TRAVERSAL) ? true : false;
     c->w = cfg->width;
     c->h = cfg->height;
     auto bail = [&](int code) { ptgpu_destroy(c); return code; };

@@ -16,7 +16,10 @@ namespace ptgpu {
 constexpr float kEps = 0.01f;                       // EPSILON, geom.h:29
 constexpr float kPi = 3.14159265358979323846f;      // FLOAT_PI, geom.h:30
 constexpr float kInfT = 1e20f;                      // Intersect's initial t
-constexpr int kStackSize = 64;                      // traversal stack entries
+#ifndef PTGPU_STACK
+#define PTGPU_STACK 64
+#endif
+constexpr int kStackSize = PTGPU_STACK;             // traversal stack entries
 
 struct f3 { float x, y, z; };
 

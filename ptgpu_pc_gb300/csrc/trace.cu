@@ -50,8 +50,11 @@ __device__ __forceinline__ uint32_t to_int(float x) {
 
 enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 
+#ifndef PTGPU_RENDER_MINBLOCKS
+#define PTGPU_RENDER_MINBLOCKS 1
+#endif
 template <bool WIDE, bool COUNT>
-__global__ void __launch_bounds__(128) k_render(const RenderArgs a, unsigned int *pixel_counter) {
+__global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const RenderArgs a, unsigned int *pixel_counter) {
     const int npx = a.width * a.height;
     const int lane = threadIdx.x & 31;
     const float inv_w = 1.f / (float)a.width, inv_h = 1.f / (float)a.height;

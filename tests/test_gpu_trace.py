@@ -110,7 +110,7 @@ def test_binary_and_wide_traversal_agree(accel, built_lib, orc):
     rays = scenes.random_rays(20_000, seed=16)
     rays["o"] = rays["o"] * np.float32(40.0) + np.array([30, 20, 60], np.float32)
     out = []
-    for flags in (0, abi.FLAG_BINARY_TRAVERSAL):
+    for flags in (0, abi.FLAG_WIDE_TRAVERSAL):
         with pt.Context(8, 8, flags=flags) as ctx:
             ctx.set_shapes(shapes, lc)
             ctx.build(accel)
