@@ -10,8 +10,9 @@
 //         the caller appends AddWallLight's nine spheres.
 //   .ply  not supported (the reference delegates to a third-party reader).
 // The format strings below are the scene-file grammar and therefore match the
-// reference's; the OBJ reader is this library's own (v and f records; faces
-// with more than three vertices are fanned into triangles).
+// reference's; the OBJ reader is this library's own (v and f records, the
+// reference reader's line rule; faces with more than three vertices are
+// fanned into triangles).
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -64,27 +65,44 @@ bool face_index(const char *tok, int32_t nverts, int32_t *out) {
     return true;
 }
 
+// Splits the file into lines the way the reference's OBJ reader does: the
+// buffer's last byte is taken for a terminator, so only lines ended by '\n',
+// '\0' or a lone '\r' before the final byte count (a file whose last line is
+// followed by a single newline loses that line, as in the reference scenes).
 bool read_obj(const char *path, Obj &obj, std::string &err) {
     FILE *f = std::fopen(path, "rb");
     if (!f) { err = std::string("cannot open model ") + path; return false; }
-    char line[4096];
+    std::string buf;
+    char chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.append(chunk, got);
+    std::fclose(f);
+    if (buf.empty()) { err = "empty model " + std::string(path); return false; }
+    const size_t end_idx = buf.size() - 1;
     std::vector<int32_t> face;
-    while (std::fgets(line, sizeof(line), f)) {
-        char *p = line;
+    size_t prev = 0;
+    for (size_t i = 0; i < end_idx; ++i) {
+        const char ch = buf[i];
+        const bool ending = ch == '\0' || ch == '\n' || (ch == '\r' && i + 1 < end_idx && buf[i + 1] != '\n');
+        if (!ending) continue;
+        std::string line = buf.substr(prev, i - prev);
+        prev = i + 1;
+        const char *p = line.c_str();
         while (*p == ' ' || *p == '\t') ++p;
         if (p[0] == 'v' && (p[1] == ' ' || p[1] == '\t')) {
             float x, y, z;
             if (std::sscanf(p + 2, "%f %f %f", &x, &y, &z) != 3) {
-                std::fclose(f); err = "malformed vertex in " + std::string(path); return false;
+                err = "malformed vertex in " + std::string(path); return false;
             }
             obj.v.push_back(x); obj.v.push_back(y); obj.v.push_back(z);
         } else if (p[0] == 'f' && (p[1] == ' ' || p[1] == '\t')) {
             face.clear();
+            std::string rest(p + 2);
             char *save = nullptr;
-            for (char *tok = strtok_r(p + 2, " \t\r\n", &save); tok; tok = strtok_r(nullptr, " \t\r\n", &save)) {
+            for (char *tok = strtok_r(&rest[0], " \t\r\n", &save); tok; tok = strtok_r(nullptr, " \t\r\n", &save)) {
                 int32_t idx;
                 if (!face_index(tok, (int32_t)(obj.v.size() / 3), &idx)) {
-                    std::fclose(f); err = "malformed face in " + std::string(path); return false;
+                    err = "malformed face in " + std::string(path); return false;
                 }
                 face.push_back(idx);
             }
@@ -93,7 +111,6 @@ bool read_obj(const char *path, Obj &obj, std::string &err) {
             }
         }
     }
-    std::fclose(f);
     return true;
 }
 

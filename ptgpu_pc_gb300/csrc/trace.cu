@@ -51,7 +51,7 @@ __device__ __forceinline__ uint32_t to_int(float x) {
 enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 
 #ifndef PTGPU_RENDER_MINBLOCKS
-#define PTGPU_RENDER_MINBLOCKS 1
+#define PTGPU_RENDER_MINBLOCKS 8   // 64 registers: 8 CTAs of 128 lanes per SM
 #endif
 template <bool WIDE, bool COUNT>
 __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const RenderArgs a, unsigned int *pixel_counter) {

@@ -1,0 +1,191 @@
+"""The library's host code (closed-form LBVH topology, KD-tree build, scene
+loader, camera, seeds) on the CPU, against the oracle and the golden
+fixtures.  Compiled without CUDA from the library's own sources."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from ptgpu_pc_gb300 import abi, scenes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+@pytest.fixture(scope="module")
+def shim(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("shim") / "libshim.so")
+    src = [os.path.join(HERE, "host", "host_shim.cpp"),
+           os.path.join(ROOT, "ptgpu_pc_gb300", "csrc", "kdtree.cpp"),
+           os.path.join(ROOT, "ptgpu_pc_gb300", "csrc", "loader.cpp")]
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                           "-o", out] + src)
+    L = ctypes.CDLL(out)
+    vp = ctypes.c_void_p
+    L.shim_topology.argtypes = [ctypes.c_int] + [vp] * 6
+    L.shim_kd_build.argtypes = [vp, ctypes.c_int, vp, vp, vp]
+    L.shim_kd_export.argtypes = [vp, ctypes.c_int64, vp]
+    L.shim_read_scene.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                                  ctypes.c_char_p, ctypes.c_int]
+    L.shim_scene_get.argtypes = [vp, vp]
+    L.shim_update_camera.argtypes = [vp]
+    L.shim_make_seeds.argtypes = [ctypes.c_uint64, vp, ctypes.c_uint32]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+@pytest.mark.parametrize("n", list(range(2, 200)) + [1000, 1023, 1024, 1025, 4097, 81934, 100003])
+def test_closed_form_topology(n, shim, orc):
+    mn, mx, g, par, leaf = (np.zeros(n - 1, np.int32) for _ in range(5))
+    lp = np.zeros(n, np.int32)
+    shim.shim_topology(n, _p(mn), _p(mx), _p(g), _p(par), _p(leaf), _p(lp))
+    btn, btl = orc.radix_tree(n)
+    assert np.array_equal(mn, btn["min"]) and np.array_equal(mx, btn["max"])
+    assert np.array_equal(g, btn["nLeft"]) and np.array_equal(g + 1, btn["nRight"])
+    assert np.array_equal(par, btn["nParent"]) and np.array_equal(leaf, btn["leaf"])
+    assert np.array_equal(lp, btl["nParent"])
+
+
+@pytest.mark.parametrize("case", ["cornell", "ico2", "ico4", "soup"])
+def test_kd_build_matches_oracle(case, shim, orc):
+    shapes = {"cornell": lambda: scenes.cornell_spheres()[0],
+              "ico2": lambda: scenes.icosphere_scene(level=2)[0],
+              "ico4": lambda: scenes.icosphere_scene(level=4)[0],
+              "soup": lambda: scenes.triangle_soup(3000, seed=9)}[case]()
+    md, sz, heap = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
+    shim.shim_kd_build(_p(shapes), len(shapes), ctypes.byref(md), ctypes.byref(sz), ctypes.byref(heap))
+    kd = orc.KD(shapes)
+    assert md.value == kd.max_depth and sz.value == kd.szbuf
+    okng, okn, ost = kd.heap()
+    if heap.value <= (1 << 20):
+        kng = np.zeros(heap.value, abi.KD_NODE)
+        kn = np.zeros(max(sz.value, 1), np.int32)
+        st = shim.shim_kd_export(_p(kng), heap.value, _p(kn))
+        assert st == ost
+        assert kng.tobytes() == okng.tobytes()
+        assert np.array_equal(kn[: sz.value], okn)
+
+
+def test_seeds_match_oracle(shim, orc):
+    a = np.zeros(1000, np.uint32)
+    shim.shim_make_seeds(1, _p(a), 1000)
+    assert np.array_equal(a, orc.make_seeds(1, 1000))
+    assert (a >= 2).all()
+
+
+def test_camera_matches_golden(shim):
+    z = np.load(os.path.join(HERE, "golden", "obj_model_scene.npz"))
+    cam = np.array(z["camera"].view(abi.CAMERA))
+    shim.shim_update_camera(_p(cam))
+    assert cam.tobytes() == z["camera_updated"].tobytes()
+
+
+def test_loader_txt_scene(shim, tmp_path):
+    """A .txt scene of this test's own: spheres, triangles and an OBJ model,
+    with the area and light-count rules of ReadTxt (displayfunc.cpp:144-505)."""
+    obj = tmp_path / "quad.obj"
+    # ends with a blank line: the reference's OBJ reader drops the final line
+    obj.write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3\nf 1/1/1 3/3/3 4/4/4\n\n")
+    scene = tmp_path / "s.txt"
+    scene.write_text("gamma 2.2  sky1 0 0 0  sky2 0 0 0\ncamera 1 2 3  4 5 6\nmaterials 1\n"
+                     "matte 0.5 0.5 0.5  0.1\nobjects 4\n"
+                     "sphere 2  0 0 0  1 1 1  0 0 0  0\n"
+                     "triangle  0 0 0  2 0 0  0 2 0  0 0 0  0.5 0.5 0.5  1\n"
+                     "model %s  10 0 0  2 3 1  0 0 0  0.2 0.3 0.4  2\n"
+                     "sphere 1  5 5 5  0 0 0  0.9 0.9 0.9  2\n" % obj)
+    n, lc, wl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    st = shim.shim_read_scene(str(scene).encode(), 64, 48, ctypes.byref(n), ctypes.byref(lc),
+                              ctypes.byref(wl), err, 256)
+    assert st == 0, err.value
+    assert n.value == 5 and lc.value == 1 and wl.value == 0
+    sh = np.zeros(n.value, abi.SHAPE)
+    cam = np.zeros(1, abi.CAMERA)
+    shim.shim_scene_get(_p(sh), _p(cam))
+    assert list(sh["type"]) == [0, 1, 1, 1, 0]
+    assert list(sh["refl"]) == [abi.DIFF, abi.SPEC, abi.REFR, abi.REFR, abi.REFR]
+    assert sh["area"][0] == np.float32(4.0) * np.float32(3.14159265358979323846) * 2 * 2
+    assert sh["area"][1] == np.float32(2.0)
+    # model vertices scaled then translated
+    assert np.array_equal(sh["p2"][2], np.array([12, 0, 0], np.float32))
+    assert cam[0]["width"] == 64 and cam[0]["height"] == 48
+    assert np.array_equal(cam[0]["orig"], np.array([1, 2, 3], np.float32))
+
+
+def test_obj_last_line_rule(shim, tmp_path):
+    """A model whose last face is followed by a single newline loses that face,
+    as the reference loader does (tinyobj treats the buffer's last byte as a
+    terminator); the reference scenes rely on it (table.obj, teapot.obj)."""
+    obj = tmp_path / "tri2.obj"
+    obj.write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nf 1 2 3\nf 3 2 1\n")
+    scene = tmp_path / "m.txt"
+    scene.write_text("camera 0 0 0  0 0 -1\nmaterials 0\nobjects 1\n"
+                     "model %s  0 0 0  1 1 1  0 0 0  0.5 0.5 0.5  0\n" % obj)
+    n, lc, wl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    assert shim.shim_read_scene(str(scene).encode(), 8, 8, ctypes.byref(n), ctypes.byref(lc),
+                                ctypes.byref(wl), err, 256) == 0
+    assert n.value == 1
+
+
+def test_loader_scn_scene_adds_wall_light(shim, tmp_path):
+    scene = tmp_path / "s.scn"
+    scene.write_text("camera 0 0 75 0 0 0\nsize 2\nsphere 3  0 0 0  0 0 0  .5 .5 .5  0\n"
+                     "sphere 1  1 1 1  4 4 4  0 0 0  1\n")
+    n, lc, wl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    st = shim.shim_read_scene(str(scene).encode(), 8, 8, ctypes.byref(n), ctypes.byref(lc),
+                              ctypes.byref(wl), err, 256)
+    assert st == 0 and wl.value == 1 and n.value == 2 + 9 and lc.value == 0
+
+
+def test_loader_errors(shim, tmp_path):
+    n, lc, wl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    assert shim.shim_read_scene(b"/nonexistent.txt", 8, 8, ctypes.byref(n), ctypes.byref(lc),
+                                ctypes.byref(wl), err, 256) == abi.E_IO
+    bad = tmp_path / "bad.txt"
+    bad.write_text("camera 1 2\n")
+    assert shim.shim_read_scene(str(bad).encode(), 8, 8, ctypes.byref(n), ctypes.byref(lc),
+                                ctypes.byref(wl), err, 256) == abi.E_IO
+    ply = tmp_path / "x.ply"
+    ply.write_text("ply\n")
+    assert shim.shim_read_scene(str(ply).encode(), 8, 8, ctypes.byref(n), ctypes.byref(lc),
+                                ctypes.byref(wl), err, 256) == abi.E_INVAL
+
+
+def test_loader_matches_reference_loader(shim):
+    """The reference scene file loaded by the reference's own loader (golden
+    fixture) and by this library give the same shapes; needs the reference's
+    model files, so it runs only where the reference tree is present."""
+    ref = os.environ.get("PTGPU_REFERENCE_DIR", "/root/reference")
+    if not os.path.isfile(os.path.join(ref, "scenes", "obj-model.txt")):
+        pytest.skip("reference scene files not present")
+    z = np.load(os.path.join(HERE, "golden", "obj_model_scene.npz"))
+    gold = z["shapes"].view(abi.SHAPE)
+    cwd = os.getcwd()
+    try:
+        os.chdir(ref)
+        n, lc, wl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        err = ctypes.create_string_buffer(256)
+        st = shim.shim_read_scene(b"scenes/obj-model.txt", 40, 30, ctypes.byref(n),
+                                  ctypes.byref(lc), ctypes.byref(wl), err, 256)
+    finally:
+        os.chdir(cwd)
+    assert st == 0 and n.value == len(gold) and lc.value == int(z["light_cnt"])
+    sh = np.zeros(n.value, abi.SHAPE)
+    cam = np.zeros(1, abi.CAMERA)
+    shim.shim_scene_get(_p(sh), _p(cam))
+    for f in ("type", "p1", "p2", "p3", "e", "c", "refl", "area"):
+        a = sh[f]
+        b = gold[f]
+        if f in ("p1", "p2", "p3"):
+            tri = sh["type"] == abi.TRIANGLE
+            a, b = a[tri], b[tri]
+        assert a.tobytes() == b.tobytes(), f
+    assert cam.tobytes()[:40] == z["camera"].tobytes()[:40]
