@@ -916,14 +916,17 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
     const int ntiles_sort = (n + kSortTile - 1) / kSortTile;
     const int ntiles = (n + kTileLeaves - 1) / kTileLeaves;
     cudaError_t e;
-    static bool attr_set = false;
+    // shared-memory opt-ins are per device
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
     const size_t smem = sizeof(SortSmem);
-    if (!attr_set) {
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
         cudaFuncSetAttribute(k_onesweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_onesweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_onesweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
-        attr_set = true;
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
     k_init_state<<<1, 256, 0, s>>>(b.state);
     e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
