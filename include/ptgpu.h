@@ -202,6 +202,23 @@ int  ptgpu_trace_closest_device(ptgpu_ctx *ctx, const ptgpu_ray *d_rays,
                                 int32_t *d_hit);
 int  ptgpu_get_stream(ptgpu_ctx *ctx, void **stream);
 
+/* ---- BVH build without device allocation ----------------------------------- */
+/* No counterpart in the reference.  The LBVH build of ptgpu_build(ctx,
+ * PTGPU_ACCEL_BVH, 0) -- same btn[n-1] / btl[n] bytes -- from n shapes in
+ * device memory into node arrays in device memory, all three allocated by the
+ * caller on the current device; no context.  For callers that may not let a
+ * library allocate device memory (an engine with its own pool or fixed budget,
+ * a frame loop that must not stall on cudaMalloc/cudaFree, a plug-in host that
+ * forbids it): intermediates live in a fixed array inside the library, so
+ * n <= 262144 (PTGPU_E_RANGE beyond).  d_btn holds at least one node when
+ * n == 1.  The first call on a device sets up that device's array; a caller
+ * that captures streams makes it before any capture.  Calls that overlap on
+ * the GPU share the array and race: serialise them.  Enqueued on `stream`
+ * (cudaStream_t, NULL = legacy default); returns after the build finished.  */
+int  ptgpu_build_bvh_noalloc(const ptgpu_shape *d_shapes, uint32_t n,
+                             ptgpu_bvh_node *d_btn, ptgpu_bvh_node *d_btl,
+                             void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

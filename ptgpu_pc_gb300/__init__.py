@@ -25,6 +25,7 @@ EXPORTS = [
     "ptgpu_draw_frame", "ptgpu_render_async", "ptgpu_synchronize", "ptgpu_get_colors",
     "ptgpu_get_pixels", "ptgpu_get_current_sample", "ptgpu_trace_closest",
     "ptgpu_trace_closest_device", "ptgpu_get_stream", "ptgpu_render_stats",
+    "ptgpu_build_bvh_noalloc",
 ]
 
 _lib = None
@@ -63,6 +64,7 @@ def lib():
         L.ptgpu_set_camera.argtypes = [vp, vp]
         L.ptgpu_get_camera.argtypes = [vp, vp]
         L.ptgpu_build.argtypes = [vp, i32, u32]
+        L.ptgpu_build_bvh_noalloc.argtypes = [vp, u32, vp, vp, vp]
         L.ptgpu_get_bvh.argtypes = [vp, vp, vp]
         L.ptgpu_set_bvh.argtypes = [vp, vp, vp, u32]
         L.ptgpu_get_kdtree.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]

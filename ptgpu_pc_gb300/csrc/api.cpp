@@ -62,6 +62,11 @@ bool viszero(const ptgpu_vec &v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f
 
 }  // namespace
 
+namespace ptgpu {
+// lets entry points outside this file report through ptgpu_last_error()
+int record_error(int code, const std::string &msg) { return fail(code, msg); }
+}  // namespace ptgpu
+
 struct ptgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
