@@ -42,6 +42,20 @@ WORKLOAD = "icosphere_81934tri_512x512_16spp_depth8_bvh"
 BUILD_FLAGS = 0x4   # PTGPU_FLAG_TREELET: the 7-leaf treelet stage of the scene's build
 
 
+def ncu_traffic(profile, key):
+    """DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one ncu
+    capture of the same workload, from the `key: value` line of its summary
+    under profiles/; None when the summary is absent."""
+    try:
+        with open(os.path.join(ROOT, "profiles", profile)) as f:
+            for line in f:
+                if line.startswith(key + ":"):
+                    return int(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -350,8 +364,10 @@ def main():
                     "per_step": "set_shapes + BVH build (with treelets) + set_seeds + draw_frame(16)"},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "k_render",
+                         "frac": achieved / hbm_peak,
+                         "traffic": ncu_traffic("k_render_icosphere81934_512x512_16spp.txt",
+                                                "traffic_bytes_per_launch"),
+                         "peak_kind": peak_kind, "kernel": "k_render",
                          "model": "per query 32 B + 60 B/node visit + 36 B/prim test, GPU-counted",
                          "bytes_per_frame": bytes_frame,
                          "counts": {"ext_queries": ext_q, "shadow_queries": sh_q,
@@ -363,8 +379,9 @@ def main():
         lb_bytes = 252 * LBVH_N
         lb_ach = lb_bytes / (lb["ms"] / 1e3) / 1e9
         lb["roofline"] = {"bound": "hbm", "achieved": lb_ach, "peak": hbm_peak, "unit": "GB/s",
-                          "frac": lb_ach / hbm_peak, "traffic": None, "peak_kind": peak_kind,
-                          "model": "252 B/triangle"}
+                          "frac": lb_ach / hbm_peak,
+                          "traffic": ncu_traffic("lbvh_build_soup4m.txt", "traffic_bytes_per_build"),
+                          "peak_kind": peak_kind, "model": "252 B/triangle, whole build"}
         line["lbvh"] = lb
         line["closest_hit"] = bench_closest(lctx, torch, scenes, 1, 3)
         lctx.close()

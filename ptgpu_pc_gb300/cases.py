@@ -1,0 +1,87 @@
+"""Fixed, seeded workloads of the hot path for profiling one kernel at a time.
+
+    python -m ptgpu_pc_gb300.cases render  [--width 512 --height 512 --spp 16 --frames 2]
+    python -m ptgpu_pc_gb300.cases lbvh    [--n 4194304 --builds 2]
+    python -m ptgpu_pc_gb300.cases closest [--n 4194304 --rays 16777216 --reps 2]
+
+render: the displaced-icosphere scene (81,934 shapes) built with treelets,
+`frames` frames of `spp` passes each through the lane tracer.  lbvh: builds of
+`n` seeded random triangles (the ptgpu_build(ctx, PTGPU_ACCEL_BVH, 0) path).
+closest: ptgpu_trace_closest_device on random rays against an LBVH of `n`
+random triangles.  Each case prints one line per repetition with its device
+time, so its launch sequence is fixed: set-up launches first, then the same
+kernels once per repetition.
+"""
+import argparse
+import time
+
+import numpy as np
+
+import ptgpu_pc_gb300 as pt
+from ptgpu_pc_gb300 import abi, scenes
+
+
+def run_render(a):
+    shapes, lc, cam = scenes.icosphere_scene(level=6)
+    with pt.Context(a.width, a.height, accel=abi.ACCEL_BVH, max_depth=a.max_depth) as ctx:
+        ctx.set_shapes(shapes, lc)
+        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET)
+        ctx.set_camera(cam)
+        ctx.set_seeds(pt.make_seeds(1, 2 * a.width * a.height))
+        for i in range(a.frames):
+            t0 = time.perf_counter()
+            ctx.reset()
+            ctx.render_async(a.spp)
+            ctx.synchronize()
+            print("render %dx%d %d spp frame %d: %.2f ms (host clock)"
+                  % (a.width, a.height, a.spp, i, (time.perf_counter() - t0) * 1e3))
+
+
+def run_lbvh(a):
+    shapes = scenes.triangle_soup(a.n, seed=3)
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, 0)
+        for i in range(a.builds):
+            ctx.build(abi.ACCEL_BVH)
+            print("lbvh n=%d build %d: %.3f ms" % (a.n, i, ctx.last_build_ms()))
+
+
+def run_closest(a):
+    import torch
+    shapes = scenes.triangle_soup(a.n, seed=3)
+    rays = scenes.random_rays(a.rays, seed=4)
+    d_rays = torch.from_numpy(rays.view(np.uint8).reshape(-1)).cuda()
+    d_t = torch.empty(a.rays, dtype=torch.float32, device="cuda")
+    d_id = torch.empty(a.rays, dtype=torch.int32, device="cuda")
+    d_hit = torch.empty(a.rays, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, 0)
+        ctx.build(abi.ACCEL_BVH)
+        for i in range(a.reps):
+            t0 = time.perf_counter()
+            ctx.trace_closest_device(d_rays.data_ptr(), a.rays, d_t.data_ptr(), d_id.data_ptr(),
+                                     d_hit.data_ptr())
+            ctx.synchronize()
+            print("closest %d rays vs %d tris rep %d: %.2f ms (host clock)"
+                  % (a.rays, a.n, i, (time.perf_counter() - t0) * 1e3))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["render", "lbvh", "closest"])
+    ap.add_argument("--width", type=int, default=512)
+    ap.add_argument("--height", type=int, default=512)
+    ap.add_argument("--spp", type=int, default=16)
+    ap.add_argument("--max-depth", type=int, default=8)
+    ap.add_argument("--frames", type=int, default=2)
+    ap.add_argument("--n", type=int, default=1 << 22)
+    ap.add_argument("--builds", type=int, default=2)
+    ap.add_argument("--rays", type=int, default=1 << 24)
+    ap.add_argument("--reps", type=int, default=2)
+    a = ap.parse_args()
+    {"render": run_render, "lbvh": run_lbvh, "closest": run_closest}[a.case](a)
+
+
+if __name__ == "__main__":
+    main()
