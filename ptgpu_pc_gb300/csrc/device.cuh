@@ -163,142 +163,179 @@ __device__ __forceinline__ float f4get(const float4 &v, int k) {
 }
 __device__ __forceinline__ int i4get(const float4 &v, int k) { return __float_as_int(f4get(v, k)); }
 
-// returns: closest query -> the reference's `intersected` (t, prim set);
-//          shadow query  -> 1 when occluded
-template <bool WIDE, bool COUNT>
-__device__ __forceinline__ int trace_query(const TraceView &tv, f3 o, f3 d, bool any, float maxt,
-                                           float &t, int &prim, Counts *cnt) {
-    prim = -1;
-    t = kInfT;
+// A query in flight: the ray, the best hit so far and the traversal
+// position (current item and stack depth; the stack itself is the caller's).
+// trav_begin sets it up, trav_step advances it by one item, so a kernel can
+// interleave the queries of its lanes with other work between steps.
+struct Trav {
+    f3 o, d, inv;
+    float tb;      // closest: best t so far; shadow: maxt
+    int prim;      // closest: traversal-order index of the best hit
+    int cur, ccnt; // current item: internal node (ccnt == 0) or leaf range
+    int sp;
+    int any, hit;  // shadow query; a hit was found (shadow: occluded)
+};
+
+// Starts a query.  Returns true when it is already answered (empty scene,
+// brute-force mode, or the root box missed).
+template <bool COUNT>
+__device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f3 d, bool any,
+                                           float maxt, Counts *cnt) {
+    q.o = o;
+    q.d = d;
+    q.any = any;
+    q.hit = 0;
+    q.prim = -1;
+    q.tb = any ? maxt : kInfT;
+    q.sp = 0;
     const int n = tv.n_shapes;
-    if (n <= 0 || (any && n <= 1)) return 0;
+    if (n <= 0 || (any && n <= 1)) return true;
     if (tv.accel == PTGPU_ACCEL_NONE) {
         if (any) {
             for (int i = n - 2; i >= 0; --i) {
                 float dd = prim_intersect(tv.prims, i, o, d);
                 if (COUNT) cnt->p++;
-                if (dd != 0.f && dd < maxt) return 1;
+                if (dd != 0.f && dd < maxt) { q.hit = 1; return true; }
             }
-            return 0;
+            return true;
         }
         for (int i = n - 1; i >= 0; --i) {
             float dd = prim_intersect(tv.prims, i, o, d);
             if (COUNT) cnt->p++;
-            if (dd != 0.f && dd < t) { t = dd; prim = i; }
+            if (dd != 0.f && dd < q.tb) { q.tb = dd; q.prim = i; }
         }
-        return t < kInfT;
+        q.hit = q.tb < kInfT;
+        return true;
     }
-    const f3 inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-    const int skip = n - 1;
-    float tb = any ? maxt : kInfT;
-    int hit_any = 0;
+    q.inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
     float tmin, tmax;
     if (!slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
-              __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, inv, tmin,
+              __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, q.inv, tmin,
               tmax))
-        return 0;
-    int stack[kStackSize];
-    int sp = 0;
-    // current item: internal node (cnt == 0) or a leaf range (cnt > 0)
-    int cur = tv.root_count > 0 ? tv.root_first : 0;
-    int ccnt = tv.root_count > 0 ? tv.root_count : 0;
-    for (;;) {
-        if (ccnt > 0) {
-            for (int k = cur; k < cur + ccnt; ++k) {
-                if (any && __ldg(&tv.prim_id[k]) == skip) continue;
-                float dd = prim_intersect(tv.prims, k, o, d);
-                if (COUNT) cnt->p++;
-                if (dd != 0.f) {
-                    if (any) {
-                        if (dd < maxt) return 1;
-                    } else {
-                        hit_any = 1;
-                        if (dd < tb) { tb = dd; prim = k; }
-                    }
+        return true;
+    q.cur = tv.root_count > 0 ? tv.root_first : 0;
+    q.ccnt = tv.root_count > 0 ? tv.root_count : 0;
+    return false;
+}
+
+// One item of the traversal: a leaf range's primitives or one node's
+// children.  Returns true when the query is answered.
+#ifndef PTGPU_TRAV_FUSE
+#define PTGPU_TRAV_FUSE 1
+#endif
+template <bool WIDE, bool COUNT>
+__device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *stack, Counts *cnt) {
+    if (q.ccnt > 0) {
+        const int skip = tv.n_shapes - 1;
+        for (int k = q.cur; k < q.cur + q.ccnt; ++k) {
+            if (q.any && __ldg(&tv.prim_id[k]) == skip) continue;
+            float dd = prim_intersect(tv.prims, k, q.o, q.d);
+            if (COUNT) cnt->p++;
+            if (dd != 0.f) {
+                if (q.any) {
+                    if (dd < q.tb) { q.hit = 1; return true; }
+                } else {
+                    q.hit = 1;
+                    if (dd < q.tb) { q.tb = dd; q.prim = k; }
                 }
             }
-        } else if (WIDE) {
-            const float4 *p = tv.nodes4 + 8 * (size_t)cur;
-            Node4 nd;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) nd.q[k] = __ldg(p + k);
-            if (COUNT) cnt->v++;
-            // hit children: leaves first in slot order, then internal nodes by distance
-            int iref[4];
-            float idist[4];
-            int ni = 0;
-            int lref[4], lcnt[4];
-            int nl = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int c = i4get(nd.q[7], k);
-                float t0, t1;
-                bool h = slab(f4get(nd.q[0], k), f4get(nd.q[1], k), f4get(nd.q[2], k),
-                              f4get(nd.q[3], k), f4get(nd.q[4], k), f4get(nd.q[5], k), o, inv, t0,
-                              t1);
-                if (c < 0 || !enter_box(h, t0, t1, tb)) continue;
-                if (c > 0) { lref[nl] = i4get(nd.q[6], k); lcnt[nl] = c; ++nl; }
-                else { iref[ni] = i4get(nd.q[6], k); idist[ni] = t0; ++ni; }
-            }
-            // internal children: sort nearest first, push the others far first
-#pragma unroll
-            for (int a = 1; a < 4; ++a) {
-                if (a < ni) {
-                    float dv = idist[a];
-                    int rv = iref[a];
-                    int b = a - 1;
-                    while (b >= 0 && idist[b] > dv) { idist[b + 1] = idist[b]; iref[b + 1] = iref[b]; --b; }
-                    idist[b + 1] = dv;
-                    iref[b + 1] = rv;
-                }
-            }
-            for (int a = ni - 1; a >= 0; --a) {
-                if (sp < kStackSize) stack[sp++] = iref[a];
-                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
-            }
-            // leaves go on the stack as negative entries, tested before the nodes
-            for (int a = nl - 1; a >= 0; --a) {
-                if (sp + 1 < kStackSize) { stack[sp++] = lcnt[a]; stack[sp++] = ~lref[a]; }
-                else if (tv.error_flags) atomicOr(tv.error_flags, 1);
-            }
-            if (sp == 0) break;
-            int e = stack[--sp];
-            if (e < 0) { cur = ~e; ccnt = stack[--sp]; }
-            else { cur = e; ccnt = 0; }
-            continue;
-        } else {
-            const float4 *nd = tv.nodes + 4 * (size_t)cur;
-            float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
-            int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
-            if (COUNT) cnt->v++;
-            float lt0, lt1, rt0, rt1;
-            bool lh = slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv, lt0, lt1);
-            bool rh = slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv, rt0, rt1);
-            lh = enter_box(lh, lt0, lt1, tb);
-            rh = enter_box(rh, rt0, rt1, tb);
-            if (lh && rh) {
-                // nearer child next, the other onto the stack (leaf: negative pair)
-                bool lfirst = !(rt0 < lt0);
-                int fr = lfirst ? q3.y : q3.x, fc = lfirst ? q3.w : q3.z;
-                int nr = lfirst ? q3.x : q3.y, nc = lfirst ? q3.z : q3.w;
-                if (sp + 1 < kStackSize) {
-                    if (fc > 0) { stack[sp++] = fc; stack[sp++] = ~fr; }
-                    else stack[sp++] = fr;
-                } else if (tv.error_flags) atomicOr(tv.error_flags, 1);
-                cur = nr; ccnt = nc;
-                continue;
-            }
-            if (lh) { cur = q3.x; ccnt = q3.z; continue; }
-            if (rh) { cur = q3.y; ccnt = q3.w; continue; }
         }
-        if (sp == 0) break;
-        int e = stack[--sp];
-        if (e < 0) { cur = ~e; ccnt = stack[--sp]; }
-        else { cur = e; ccnt = 0; }
+        if (q.sp == 0) return true;
+        int e = stack[--q.sp];
+        if (e < 0) { q.cur = ~e; q.ccnt = stack[--q.sp]; }
+        else { q.cur = e; q.ccnt = 0; }
+        // a node popped after a leaf is visited in the same step, so lanes
+        // at a leaf and lanes at a node share the node half of the step
+        if (!PTGPU_TRAV_FUSE || q.ccnt > 0) return false;
     }
-    if (any) return 0;
-    t = tb;
-    return hit_any;
+    if (WIDE) {
+        const float4 *p = tv.nodes4 + 8 * (size_t)q.cur;
+        Node4 nd;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) nd.q[k] = __ldg(p + k);
+        if (COUNT) cnt->v++;
+        // hit children: leaves first in slot order, then internal nodes by distance
+        int iref[4];
+        float idist[4];
+        int ni = 0;
+        int lref[4], lcnt[4];
+        int nl = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = i4get(nd.q[7], k);
+            float t0, t1;
+            bool h = slab(f4get(nd.q[0], k), f4get(nd.q[1], k), f4get(nd.q[2], k),
+                          f4get(nd.q[3], k), f4get(nd.q[4], k), f4get(nd.q[5], k), q.o, q.inv, t0,
+                          t1);
+            if (c < 0 || !enter_box(h, t0, t1, q.tb)) continue;
+            if (c > 0) { lref[nl] = i4get(nd.q[6], k); lcnt[nl] = c; ++nl; }
+            else { iref[ni] = i4get(nd.q[6], k); idist[ni] = t0; ++ni; }
+        }
+        // internal children: sort nearest first, push the others far first
+#pragma unroll
+        for (int a = 1; a < 4; ++a) {
+            if (a < ni) {
+                float dv = idist[a];
+                int rv = iref[a];
+                int b = a - 1;
+                while (b >= 0 && idist[b] > dv) { idist[b + 1] = idist[b]; iref[b + 1] = iref[b]; --b; }
+                idist[b + 1] = dv;
+                iref[b + 1] = rv;
+            }
+        }
+        for (int a = ni - 1; a >= 0; --a) {
+            if (q.sp < kStackSize) stack[q.sp++] = iref[a];
+            else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+        }
+        // leaves go on the stack as negative entries, tested before the nodes
+        for (int a = nl - 1; a >= 0; --a) {
+            if (q.sp + 1 < kStackSize) { stack[q.sp++] = lcnt[a]; stack[q.sp++] = ~lref[a]; }
+            else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+        }
+    } else {
+        const float4 *nd = tv.nodes + 4 * (size_t)q.cur;
+        float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+        int4 q3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+        if (COUNT) cnt->v++;
+        float lt0, lt1, rt0, rt1;
+        bool lh = slab(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q.o, q.inv, lt0, lt1);
+        bool rh = slab(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, q.o, q.inv, rt0, rt1);
+        lh = enter_box(lh, lt0, lt1, q.tb);
+        rh = enter_box(rh, rt0, rt1, q.tb);
+        if (lh && rh) {
+            // nearer child next, the other onto the stack (leaf: negative pair)
+            bool lfirst = !(rt0 < lt0);
+            int fr = lfirst ? q3.y : q3.x, fc = lfirst ? q3.w : q3.z;
+            int nr = lfirst ? q3.x : q3.y, nc = lfirst ? q3.z : q3.w;
+            if (q.sp + 1 < kStackSize) {
+                if (fc > 0) { stack[q.sp++] = fc; stack[q.sp++] = ~fr; }
+                else stack[q.sp++] = fr;
+            } else if (tv.error_flags) atomicOr(tv.error_flags, 1);
+            q.cur = nr; q.ccnt = nc;
+            return false;
+        }
+        if (lh) { q.cur = q3.x; q.ccnt = q3.z; return false; }
+        if (rh) { q.cur = q3.y; q.ccnt = q3.w; return false; }
+    }
+    if (q.sp == 0) return true;
+    int e = stack[--q.sp];
+    if (e < 0) { q.cur = ~e; q.ccnt = stack[--q.sp]; }
+    else { q.cur = e; q.ccnt = 0; }
+    return false;
+}
+
+// A whole query.  Returns: closest query -> the reference's `intersected`
+// (t, prim set); shadow query -> 1 when occluded.
+template <bool WIDE, bool COUNT>
+__device__ __forceinline__ int trace_query(const TraceView &tv, f3 o, f3 d, bool any, float maxt,
+                                           float &t, int &prim, Counts *cnt) {
+    Trav q;
+    int stack[kStackSize];
+    if (!trav_begin<COUNT>(tv, q, o, d, any, maxt, cnt))
+        while (!trav_step<WIDE, COUNT>(tv, q, stack, cnt)) {}
+    t = any ? kInfT : q.tb;
+    prim = q.prim;
+    return q.hit;
 }
 
 }  // namespace ptgpu

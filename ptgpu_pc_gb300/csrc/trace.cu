@@ -2,11 +2,16 @@
 //
 // The tracer (RadianceGPU, rendering_kernel.cl:1072-1150, with
 // RadiancePathTracing / RadianceOnePathTracing / SampleLights) runs as a
-// per-lane state machine: every iteration of the kernel's loop each lane
-// issues exactly one ray query -- an extension ray or one light's shadow
-// ray -- through a single traversal routine, then consumes its result.
-// Lanes of a warp therefore run the traversal together instead of drifting
-// apart inside nested per-pass / per-bounce / per-light loops.  A lane that
+// per-lane state machine around one resumable traversal.  Each lane has at
+// most one ray query in flight -- an extension ray or one light's shadow ray
+// -- held in a Trav record with its own stack.  A warp advances its queries
+// one traversal step (a leaf's primitives, then a node's children) at a
+// time, and leaves the stepping loop only when a set share of its live
+// lanes (PTGPU_RENDER_REFILL / 32) has an answered query or none: those
+// lanes then consume their answers and start their next queries together,
+// while the other lanes keep their place in their traversals.  Lanes thus
+// stay busy in the traversal instead of idling until the warp's longest
+// query ends, and the shading code runs for many lanes at once.  A lane that
 // has finished all passes of its pixel takes the next pixel from a global
 // counter: the lanes that need work vote (ballot), one atomicAdd reserves a
 // contiguous run, and each lane's slot is its prefix popcount in the vote.
@@ -14,9 +19,11 @@
 // A pixel's passes are sequential by construction -- each continues the
 // pixel's seed stream where the previous one stopped -- so one lane runs all
 // of a pixel's passes and keeps its seeds and running mean in registers.
-// Deferring a shadow query to the next loop iteration changes no random
-// draw: SampleLights consumes its two randoms before the visibility test, and
-// the light contributions are summed in light order as in the reference.
+// Deferring a query changes no random draw and no result: SampleLights
+// consumes its two randoms before the visibility test, the light
+// contributions are summed in light order as in the reference, and every
+// query visits its nodes in the same order whether it runs in one go or in
+// steps.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -51,7 +58,17 @@ __device__ __forceinline__ uint32_t to_int(float x) {
 enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 
 #ifndef PTGPU_RENDER_MINBLOCKS
-#define PTGPU_RENDER_MINBLOCKS 8   // 64 registers: 8 CTAs of 128 lanes per SM
+#define PTGPU_RENDER_MINBLOCKS 7   // 72 registers: 7 CTAs of 128 lanes per SM
+#endif
+// A warp leaves its traversal steps to shade when at least this many 32nds
+// of its live lanes wait without a query in flight (32: when every query of
+// the warp is answered).
+#ifndef PTGPU_RENDER_REFILL
+#define PTGPU_RENDER_REFILL 20
+#endif
+// traversal steps between two looks at the warp's waiting lanes
+#ifndef PTGPU_RENDER_STEPS
+#define PTGPU_RENDER_STEPS 1
 #endif
 template <bool WIDE, bool COUNT>
 __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const RenderArgs a, unsigned int *pixel_counter) {
@@ -61,12 +78,22 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     int state = ST_NEED;
     int gid = 0, passes_done = 0, depth = 0, li = 0, specular = 1;
     uint32_t s0 = 0, s1 = 0;
-    f3 col = mk3(0.f, 0.f, 0.f), o = col, d = col, rad = col, tp = col, hp = col, nl = col;
+    f3 col = mk3(0.f, 0.f, 0.f), rad = col, tp = col, hp = col, nl = col;
     f3 ld = col, pend = col;
-    f3 qo = col, qd = col;
-    float qmax = 0.f;
-    bool qany = false;
+    Trav q;
+    q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
+    q.any = 0; q.hit = 0;
+    int stack[kStackSize];
+    bool trav = false;   // a query in flight
+    bool fin = false;    // an answered query not yet consumed
     Counts cnt[3] = {{0, 0}, {0, 0}, {0, 0}};
+
+    // starts a query; an immediately answered one is consumed like any other
+    auto start = [&](f3 o, f3 d, bool any, float maxt) {
+        Counts *c = cnt + (any ? 1 : 0);
+        if (trav_begin<COUNT>(a.tv, q, o, d, any, maxt, c)) fin = true;
+        else trav = true;
+    };
 
     for (;;) {
         // ---- refill lanes that finished their pixel
@@ -96,116 +123,132 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
         }
         if (__all_sync(0xffffffffu, state == ST_DONE)) break;
 
-        // ---- produce this lane's query
-        bool has_q = false;
-        if (state == ST_GEN) {
-            // GenerateCameraRay (rendering_kernel.cl:1042-1070)
-            const int x = gid % a.width, y = gid / a.width;
-            const ptgpu_camera &cam = a.cam;
-            const float r1 = get_random(s0, s1) - .5f;
-            const float r2 = get_random(s0, s1) - .5f;
-            const float kcx = ((float)x + r1) * inv_w - .5f;
-            const float kcy = ((float)y + r2) * inv_h - .5f;
-            f3 rdir = mk3(cam.x.x * kcx + cam.y.x * kcy + cam.dir.x,
-                          cam.x.y * kcx + cam.y.y * kcy + cam.dir.y,
-                          cam.x.z * kcx + cam.y.z * kcy + cam.dir.z);
-            o = add3(smul3(0.1f, rdir), mk3(cam.orig.x, cam.orig.y, cam.orig.z));
-            d = norm3(rdir);
-            rad = mk3(0.f, 0.f, 0.f);
-            tp = mk3(1.f, 1.f, 1.f);
-            specular = 1;
-            depth = 0;
-            state = ST_EXT;
+        // ---- lanes without a query: produce the next one
+        if (!trav && !fin) {
+            if (state == ST_GEN) {
+                // GenerateCameraRay (rendering_kernel.cl:1042-1070)
+                const int x = gid % a.width, y = gid / a.width;
+                const ptgpu_camera &cam = a.cam;
+                const float r1 = get_random(s0, s1) - .5f;
+                const float r2 = get_random(s0, s1) - .5f;
+                const float kcx = ((float)x + r1) * inv_w - .5f;
+                const float kcy = ((float)y + r2) * inv_h - .5f;
+                f3 rdir = mk3(cam.x.x * kcx + cam.y.x * kcy + cam.dir.x,
+                              cam.x.y * kcx + cam.y.y * kcy + cam.dir.y,
+                              cam.x.z * kcx + cam.y.z * kcy + cam.dir.z);
+                const f3 o = add3(smul3(0.1f, rdir), mk3(cam.orig.x, cam.orig.y, cam.orig.z));
+                rad = mk3(0.f, 0.f, 0.f);
+                tp = mk3(1.f, 1.f, 1.f);
+                specular = 1;
+                depth = 0;
+                state = ST_EXT;
+                if (COUNT) cnt[2].p++;
+                start(o, norm3(rdir), false, 0.f);
+            } else if (state == ST_NEE) {
+                // SampleLights (rendering_kernel.cl:397-493): the next light
+                // that needs a visibility test
+                bool has_q = false;
+                while (li < a.n_lights) {
+                    const LightRec L = a.lights[li];
+                    float u1, u2;
+                    if (a.rtl) { u2 = get_random(s0, s1); u1 = get_random(s0, s1); }
+                    else       { u1 = get_random(s0, s1); u2 = get_random(s0, s1); }
+                    f3 lp, lnrm;
+                    if (__float_as_int(L.a.w) == PTGPU_TRIANGLE) {
+                        const float su1 = sqrtf(u1);
+                        const float bu = 1.0f - su1, bv = u2 * su1;
+                        const f3 e1 = smul3(bu, mk3(L.b.x, L.b.y, L.b.z));
+                        const f3 e2 = smul3(bv, mk3(L.c.x, L.c.y, L.c.z));
+                        lp = add3(add3(mk3(L.a.x, L.a.y, L.a.z), e1), e2);
+                        lnrm = norm3(cross3(e1, e2));
+                    } else {
+                        const float zz = 1.f - 2.f * u1;
+                        const float rr = sqrtf(fmaxf(0.f, 1.f - zz * zz));
+                        const float phi = 2.f * kPi * u2;
+                        float sphi, cphi;
+                        pt_sincos(phi, sphi, cphi);
+                        const f3 unit = mk3(rr * cphi, rr * sphi, zz);
+                        lp = add3(smul3(L.b.x, unit), mk3(L.a.x, L.a.y, L.a.z));
+                        lnrm = unit;
+                    }
+                    f3 sd = sub3(lp, hp);
+                    const float len = sqrtf(dot3(sd, sd));
+                    sd = smul3(1.f / len, sd);
+                    float wo = dot3(sd, lnrm);
+                    if (wo > 0.f) { ++li; continue; }
+                    wo = -wo;
+                    wo = cl_clamp(wo, 0.f, 1.f);
+                    const float wi = dot3(sd, nl);
+                    if (wi > 0.f) {
+                        const float s = L.b.w * wi * wo / (len * len);
+                        pend = smul3(s, mk3(L.e.x, L.e.y, L.e.z));
+                        has_q = true;
+                        if (COUNT) cnt[2].v++;
+                        start(hp, sd, true, len - kEps);
+                        break;
+                    }
+                    ++li;
+                }
+                if (!has_q) {
+                    // all lights done: Ld * throughput, then the diffuse bounce
+                    ld = mul3(ld, tp);
+                    rad = add3(rad, ld);
+                    const float r1 = 2.f * kPi * get_random(s0, s1);
+                    const float r2 = get_random(s0, s1);
+                    const float r2s = sqrtf(r2);
+                    f3 w = nl;
+                    const f3 av = (fabsf(w.x) > .1f) ? mk3(0.f, 1.f, 0.f) : mk3(1.f, 0.f, 0.f);
+                    f3 u = norm3(cross3(av, w));
+                    f3 v = cross3(w, u);
+                    float sr1, cr1;
+                    pt_sincos(r1, sr1, cr1);
+                    u = smul3(cr1 * r2s, u);
+                    v = smul3(sr1 * r2s, v);
+                    f3 nd = add3(u, v);
+                    w = smul3(sqrtf(1.f - r2), w);
+                    nd = add3(nd, w);
+                    if (++depth > a.max_depth) {
+                        state = -1;   // pass finished
+                    } else {
+                        state = ST_EXT;
+                        if (COUNT) cnt[2].p++;
+                        start(hp, nd, false, 0.f);
+                    }
+                }
+            }
         }
-        if (state == ST_NEE) {
-            // SampleLights (rendering_kernel.cl:397-493): the next light that
-            // needs a visibility test
-            while (li < a.n_lights) {
-                const LightRec L = a.lights[li];
-                float u1, u2;
-                if (a.rtl) { u2 = get_random(s0, s1); u1 = get_random(s0, s1); }
-                else       { u1 = get_random(s0, s1); u2 = get_random(s0, s1); }
-                f3 lp, lnrm;
-                if (__float_as_int(L.a.w) == PTGPU_TRIANGLE) {
-                    const float su1 = sqrtf(u1);
-                    const float bu = 1.0f - su1, bv = u2 * su1;
-                    const f3 e1 = smul3(bu, mk3(L.b.x, L.b.y, L.b.z));
-                    const f3 e2 = smul3(bv, mk3(L.c.x, L.c.y, L.c.z));
-                    lp = add3(add3(mk3(L.a.x, L.a.y, L.a.z), e1), e2);
-                    lnrm = norm3(cross3(e1, e2));
-                } else {
-                    const float zz = 1.f - 2.f * u1;
-                    const float rr = sqrtf(fmaxf(0.f, 1.f - zz * zz));
-                    const float phi = 2.f * kPi * u2;
-                    float sphi, cphi;
-                    pt_sincos(phi, sphi, cphi);
-                    const f3 unit = mk3(rr * cphi, rr * sphi, zz);
-                    lp = add3(smul3(L.b.x, unit), mk3(L.a.x, L.a.y, L.a.z));
-                    lnrm = unit;
-                }
-                f3 sd = sub3(lp, hp);
-                const float len = sqrtf(dot3(sd, sd));
-                sd = smul3(1.f / len, sd);
-                float wo = dot3(sd, lnrm);
-                if (wo > 0.f) { ++li; continue; }
-                wo = -wo;
-                wo = cl_clamp(wo, 0.f, 1.f);
-                const float wi = dot3(sd, nl);
-                if (wi > 0.f) {
-                    const float s = L.b.w * wi * wo / (len * len);
-                    pend = smul3(s, mk3(L.e.x, L.e.y, L.e.z));
-                    qo = hp; qd = sd; qmax = len - kEps; qany = true;
-                    has_q = true;
-                    if (COUNT) cnt[2].v++;
-                    break;
-                }
+
+        // ---- traversal steps, until enough lanes wait to be served
+        for (;;) {
+            const unsigned busy = __ballot_sync(0xffffffffu, trav);
+            if (!busy) break;
+            const unsigned live = __ballot_sync(0xffffffffu, state != ST_DONE);
+            if (__popc(live & ~busy) * 32 >= PTGPU_RENDER_REFILL * __popc(live)) break;
+            if (trav && trav_step<WIDE, COUNT>(a.tv, q, stack, cnt + q.any)) {
+                trav = false;
+                fin = true;
+            }
+#if PTGPU_RENDER_STEPS > 1
+            if (trav && trav_step<WIDE, COUNT>(a.tv, q, stack, cnt + q.any)) {
+                trav = false;
+                fin = true;
+            }
+#endif
+        }
+
+        // ---- consume answered queries
+        if (fin) {
+            fin = false;
+            if (q.any) {
+                if (!q.hit) ld = add3(ld, pend);
                 ++li;
-            }
-            if (!has_q) {
-                // all lights done: Ld * throughput, then the diffuse bounce
-                ld = mul3(ld, tp);
-                rad = add3(rad, ld);
-                const float r1 = 2.f * kPi * get_random(s0, s1);
-                const float r2 = get_random(s0, s1);
-                const float r2s = sqrtf(r2);
-                f3 w = nl;
-                const f3 av = (fabsf(w.x) > .1f) ? mk3(0.f, 1.f, 0.f) : mk3(1.f, 0.f, 0.f);
-                f3 u = norm3(cross3(av, w));
-                f3 v = cross3(w, u);
-                float sr1, cr1;
-                pt_sincos(r1, sr1, cr1);
-                u = smul3(cr1 * r2s, u);
-                v = smul3(sr1 * r2s, v);
-                f3 nd = add3(u, v);
-                w = smul3(sqrtf(1.f - r2), w);
-                nd = add3(nd, w);
-                o = hp;
-                d = nd;
-                state = ++depth > a.max_depth ? -1 : ST_EXT;   // -1: pass finished
-            }
-        }
-        if (state == ST_EXT) {
-            qo = o; qd = d; qany = false; has_q = true;
-            if (COUNT) cnt[2].p++;
-        }
-
-        // ---- the query
-        float t = 0.f;
-        int prim = -1;
-        int hit = 0;
-        if (has_q)
-            hit = trace_query<WIDE, COUNT>(a.tv, qo, qd, qany, qmax, t, prim, cnt + (qany ? 1 : 0));
-
-        // ---- consume it
-        if (has_q && qany) {
-            if (!hit) ld = add3(ld, pend);
-            ++li;
-        } else if (has_q) {
-            // RadianceOnePathTracing (rendering_kernel.cl:495-753)
-            if (!hit) {
+            } else if (!q.hit) {
+                // RadianceOnePathTracing (rendering_kernel.cl:495-753)
                 state = -1;
             } else {
-                hp = add3(o, smul3(t, d));
+                const f3 d = q.d;
+                hp = add3(q.o, smul3(q.tb, d));
+                const int prim = q.prim;
                 const int id = prim >= 0 ? __ldg(&a.tv.prim_id[prim]) : 0;
                 const Material m = a.mats[id];
                 const int type = __float_as_int(m.e_type.w);
@@ -240,50 +283,51 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                     ld = mk3(0.f, 0.f, 0.f);
                     li = 0;
                     state = ST_NEE;
-                } else if (refl == PTGPU_SPEC) {
-                    specular = 1;
-                    const f3 ndir = sub3(d, smul3(2.f * dot3(normal, d), normal));
-                    tp = mul3(tp, colr);
-                    o = hp;
-                    d = ndir;
-                    state = ++depth > a.max_depth ? -1 : ST_EXT;
                 } else {
                     specular = 1;
-                    const f3 refl_d = sub3(d, smul3(2.f * dot3(normal, d), normal));
-                    const bool into = dot3(normal, nl) > 0;
-                    const float nc = 1.f, nt = 1.5f;
-                    const float nnt = into ? nc / nt : nt / nc;
-                    const float ddn = dot3(d, nl);
-                    const float cos2t = 1.f - nnt * nnt * (1.f - ddn * ddn);
-                    if (cos2t < 0.f) {
+                    f3 nd;
+                    if (refl == PTGPU_SPEC) {
+                        nd = sub3(d, smul3(2.f * dot3(normal, d), normal));
                         tp = mul3(tp, colr);
-                        o = hp;
-                        d = refl_d;
                     } else {
-                        const float kk = (float)(into ? 1 : -1) * (ddn * nnt + sqrtf(cos2t));
-                        const f3 nkk = smul3(kk, normal);
-                        const f3 tdir = norm3(sub3(smul3(nnt, d), nkk));
-                        const float aa = nt - nc, bb = nt + nc;
-                        const float R0 = aa * aa / (bb * bb);
-                        const float c = 1.f - (into ? -ddn : dot3(tdir, normal));
-                        const float Re = R0 + (1.f - R0) * c * c * c * c * c;
-                        const float Tr = 1.f - Re;
-                        const float P = .25f + .5f * Re;
-                        const float RP = Re / P;
-                        const float TP = Tr / (1.f - P);
-                        if (get_random(s0, s1) < P) {
-                            tp = smul3(RP, tp);
+                        const f3 refl_d = sub3(d, smul3(2.f * dot3(normal, d), normal));
+                        const bool into = dot3(normal, nl) > 0;
+                        const float nc = 1.f, nt = 1.5f;
+                        const float nnt = into ? nc / nt : nt / nc;
+                        const float ddn = dot3(d, nl);
+                        const float cos2t = 1.f - nnt * nnt * (1.f - ddn * ddn);
+                        if (cos2t < 0.f) {
                             tp = mul3(tp, colr);
-                            o = hp;
-                            d = refl_d;
+                            nd = refl_d;
                         } else {
-                            tp = smul3(TP, tp);
-                            tp = mul3(tp, colr);
-                            o = hp;
-                            d = tdir;
+                            const float kk = (float)(into ? 1 : -1) * (ddn * nnt + sqrtf(cos2t));
+                            const f3 nkk = smul3(kk, normal);
+                            const f3 tdir = norm3(sub3(smul3(nnt, d), nkk));
+                            const float aa = nt - nc, bb = nt + nc;
+                            const float R0 = aa * aa / (bb * bb);
+                            const float c = 1.f - (into ? -ddn : dot3(tdir, normal));
+                            const float Re = R0 + (1.f - R0) * c * c * c * c * c;
+                            const float Tr = 1.f - Re;
+                            const float P = .25f + .5f * Re;
+                            const float RP = Re / P;
+                            const float TP = Tr / (1.f - P);
+                            if (get_random(s0, s1) < P) {
+                                tp = smul3(RP, tp);
+                                tp = mul3(tp, colr);
+                                nd = refl_d;
+                            } else {
+                                tp = smul3(TP, tp);
+                                tp = mul3(tp, colr);
+                                nd = tdir;
+                            }
                         }
                     }
-                    state = ++depth > a.max_depth ? -1 : ST_EXT;
+                    if (++depth > a.max_depth) {
+                        state = -1;
+                    } else {
+                        if (COUNT) cnt[2].p++;
+                        start(hp, nd, false, 0.f);
+                    }
                 }
             }
         }
@@ -341,6 +385,9 @@ cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render<false, false>, block, 0);
     int resident = per_sm * sms;
     if (a.max_ctas > 0 && resident > a.max_ctas) resident = a.max_ctas;
+#ifdef PTGPU_RENDER_GRID
+    if (resident > PTGPU_RENDER_GRID) resident = PTGPU_RENDER_GRID;
+#endif
     if (resident > 0 && grid > resident) grid = resident;
     if (a.stats) {
         if (wide) k_render<true, true><<<grid, block, 0, s>>>(a, a.pixel_counter);
