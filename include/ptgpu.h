@@ -121,6 +121,10 @@ typedef struct {
                                          right-to-left (the order g++ gives the
                                          reference source; the default is the
                                          left-to-right order of OpenCL/clang)   */
+/* build flag field: rounds of the treelet stage (bits 8-11; 0 = one round,
+ * the single launch of CLBVH::optimize, CLBVH.cpp:318-350).  Each round runs
+ * over the tree the previous one left; Karras & Aila use three. */
+#define PTGPU_TREELET_SWEEPS(n)  ((uint32_t)((n) & 0xF) << 8)
 
 int  ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out);
 int  ptgpu_destroy(ptgpu_ctx *ctx);

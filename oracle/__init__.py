@@ -73,6 +73,7 @@ def lib():
         L.orc_sah_cost.restype = ctypes.c_double
         L.orc_sah_cost.argtypes = [u32, vp, vp]
         L.orc_treelet_optimize.argtypes = [u32, vp, vp]
+        L.orc_treelet_optimize_sweeps.argtypes = [u32, vp, vp, ctypes.c_int]
         L.orc_kd_build.argtypes = [vp, u32, ctypes.POINTER(KdTree)]
         L.orc_kd_free.argtypes = [ctypes.POINTER(KdTree)]
         L.orc_kd_heap.restype = i32
@@ -254,9 +255,9 @@ def sah_cost(btn, btl):
     return lib().orc_sah_cost(len(btl), _ptr(btn), _ptr(btl))
 
 
-def treelet_optimize(btn, btl):
+def treelet_optimize(btn, btl, sweeps=1):
     btn = btn.copy(); btl = btl.copy()
-    lib().orc_treelet_optimize(len(btl), _ptr(btn), _ptr(btl))
+    lib().orc_treelet_optimize_sweeps(len(btl), _ptr(btn), _ptr(btl), sweeps)
     return btn, btl
 
 

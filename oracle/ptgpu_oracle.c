@@ -850,10 +850,11 @@ static void treelet_rec(int nd, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, float 
     treelet_at(nd, btn, btl, cost, leaf_cost);
 }
 
-/* Sequential bottom-up treelet pass (one sweep).  After it, internal nodes
- * mark leaf children with min == nLeft / max == nRight and internal children
- * with -1 in min/max; leaf==2 still flags "has a leaf child". */
-int orc_treelet_optimize(uint32_t n, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl) {
+/* Sequential bottom-up treelet passes (`sweeps` of them, each over the tree
+ * the previous one left).  After them, internal nodes mark leaf children with
+ * min == nLeft / max == nRight and internal children with -1 in min/max;
+ * leaf==2 still flags "has a leaf child". */
+int orc_treelet_optimize_sweeps(uint32_t n, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int sweeps) {
     if (n < 3) return PTGPU_OK;
     float *cost = (float *)calloc(n, sizeof(float));
     float *leaf_cost = (float *)calloc(n, sizeof(float));
@@ -865,10 +866,14 @@ int orc_treelet_optimize(uint32_t n, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl) {
         p->min = lleaf ? p->nLeft : -1;
         p->max = rleaf ? p->nRight : -1;
     }
-    treelet_rec(0, btn, btl, cost, leaf_cost);
+    for (int it = 0; it < sweeps; it++) treelet_rec(0, btn, btl, cost, leaf_cost);
     for (uint32_t i = 0; i + 1 < n; i++) { btn[i].cost = cost[i]; btn[i].area = bound_area(&btn[i].bound); }
     free(cost); free(leaf_cost);
     return PTGPU_OK;
+}
+
+int orc_treelet_optimize(uint32_t n, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl) {
+    return orc_treelet_optimize_sweeps(n, btn, btl, 1);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -82,6 +82,7 @@ int   orc_build_bvh(ptgpu_shape *shapes, uint32_t n, ptgpu_bvh_node *btn,
                     ptgpu_bvh_node *btl, int32_t *sorted);
 double orc_sah_cost(uint32_t n, const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl);
 int   orc_treelet_optimize(uint32_t n, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl);
+int   orc_treelet_optimize_sweeps(uint32_t n, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int sweeps);
 
 /* KD tree (pointer tree arrays, nodes numbered in creation order, root 0) */
 typedef struct {

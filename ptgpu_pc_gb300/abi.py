@@ -66,6 +66,11 @@ FLAG_ARGS_RTL = 0x8
 FLAG_WIDE_TRAVERSAL = 0x10
 
 
+def treelet_sweeps(n):
+    """Build flag field: rounds of the treelet stage (0 or 1 = one round)."""
+    return (n & 0xF) << 8
+
+
 def triangles(p1, p2, p3, e=(0.0, 0.0, 0.0), c=(0.75, 0.75, 0.75), refl=DIFF):
     """Shape array of triangles with per-shape or shared emission/colour."""
     p1 = np.asarray(p1, np.float32).reshape(-1, 3)

@@ -1,10 +1,10 @@
 """Fixed, seeded workloads of the hot path for profiling one kernel at a time.
 
-    python -m ptgpu_pc_gb300.cases render  [--width 512 --height 512 --spp 16 --frames 2]
+    python -m ptgpu_pc_gb300.cases render  [--width 512 --height 512 --spp 16 --frames 2 --flags 0 --sweeps 2]
     python -m ptgpu_pc_gb300.cases lbvh    [--n 4194304 --builds 2]
     python -m ptgpu_pc_gb300.cases closest [--n 4194304 --rays 16777216 --reps 2]
 
-render: the displaced-icosphere scene (81,934 shapes) built with treelets,
+render: the displaced-icosphere scene (81,934 shapes) built with `sweeps` treelet rounds,
 `frames` frames of `spp` passes each through the lane tracer.  lbvh: builds of
 `n` seeded random triangles (the ptgpu_build(ctx, PTGPU_ACCEL_BVH, 0) path).
 closest: ptgpu_trace_closest_device on random rays against an LBVH of `n`
@@ -23,9 +23,11 @@ from ptgpu_pc_gb300 import abi, scenes
 
 def run_render(a):
     shapes, lc, cam = scenes.icosphere_scene(level=6)
-    with pt.Context(a.width, a.height, accel=abi.ACCEL_BVH, max_depth=a.max_depth) as ctx:
+    with pt.Context(a.width, a.height, accel=abi.ACCEL_BVH, max_depth=a.max_depth,
+                    flags=a.flags) as ctx:
         ctx.set_shapes(shapes, lc)
-        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET)
+        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET | abi.treelet_sweeps(a.sweeps))
+        print("scene build %.3f ms" % ctx.last_build_ms())
         ctx.set_camera(cam)
         ctx.set_seeds(pt.make_seeds(1, 2 * a.width * a.height))
         for i in range(a.frames):
@@ -75,6 +77,8 @@ def main():
     ap.add_argument("--spp", type=int, default=16)
     ap.add_argument("--max-depth", type=int, default=8)
     ap.add_argument("--frames", type=int, default=2)
+    ap.add_argument("--flags", type=int, default=0, help="ptgpu_config.flags of the render context")
+    ap.add_argument("--sweeps", type=int, default=2, help="treelet rounds of the scene build")
     ap.add_argument("--n", type=int, default=1 << 22)
     ap.add_argument("--builds", type=int, default=2)
     ap.add_argument("--rays", type=int, default=1 << 24)

@@ -369,7 +369,7 @@ static int ensure_bvh_buffers(ptgpu_ctx *c) {
 }
 
 static int prepare_wide(ptgpu_ctx *c) {
-    if (c->n_internal <= 0) return PTGPU_OK;
+    if (!c->wide || c->n_internal <= 0) return PTGPU_OK;   // 4-wide nodes only when traversed
     CK(c->d_nodes4.ensure((size_t)c->n_internal * 8 * sizeof(float4)));
     CK(launch_collapse4(c->d_nodes.as<float4>(), c->n_internal, c->d_nodes4.as<float4>(), c->stream));
     return PTGPU_OK;
@@ -431,8 +431,9 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
         if (flags & PTGPU_FLAG_TREELET) {
             CK(c->d_tcount.ensure((c->n > 1 ? c->n - 1 : 1) * sizeof(int)));
             CK(c->d_tcost.ensure((c->n > 1 ? c->n - 1 : 1) * sizeof(float)));
+            const int sweeps = (flags >> 8) & 0xF;
             CK(launch_treelet(b.btn, b.btl, (int)c->n, c->d_tcount.as<int>(), c->d_tcost.as<float>(),
-                              1, c->stream));
+                              sweeps > 0 ? sweeps : 1, c->stream));
         }
         CK(cudaEventRecord(c->ev1, c->stream));
         BuildState hs;

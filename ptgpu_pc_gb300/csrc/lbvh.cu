@@ -621,85 +621,183 @@ __global__ void k_treelet_prepare(ptgpu_bvh_node *btn, int n, int *counters) {
     counters[i] = 0;
 }
 
-__device__ void treelet_at(int root, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, float *cost) {
-    int leaves[7], nodes[6];
-    int nl = 0, nn = 0;
-    {
-        const NodeL r = load_node(btn, root);
-        leaves[nl++] = child_ref(r, false);
-        leaves[nl++] = child_ref(r, true);
+// Subsets of 7 leaves ordered by (size, value); kSubsetStart[k] is where the
+// subsets of size k begin.  Within a size the first C(nl, k) entries are the
+// subsets of the first nl leaves.
+__device__ const unsigned char kSubsets[127] = {
+    1, 2, 4, 8, 16, 32, 64,
+    3, 5, 6, 9, 10, 12, 17, 18, 20, 24, 33, 34, 36, 40, 48, 65, 66, 68, 72, 80, 96,
+    7, 11, 13, 14, 19, 21, 22, 25, 26, 28, 35, 37, 38, 41, 42, 44, 49, 50, 52, 56, 67, 69, 70,
+    73, 74, 76, 81, 82, 84, 88, 97, 98, 100, 104, 112,
+    15, 23, 27, 29, 30, 39, 43, 45, 46, 51, 53, 54, 57, 58, 60, 71, 75, 77, 78, 83, 85, 86, 89,
+    90, 92, 99, 101, 102, 105, 106, 108, 113, 114, 116, 120,
+    31, 47, 55, 59, 61, 62, 79, 87, 91, 93, 94, 103, 107, 109, 110, 115, 117, 118, 121, 122, 124,
+    63, 95, 111, 119, 123, 125, 126,
+    127};
+__device__ const unsigned char kSubsetStart[8] = {0, 0, 7, 28, 63, 98, 119, 126};
+
+__device__ const unsigned char kBinom7[8][8] = {   // C(n, k), n, k <= 7
+    {1, 0, 0, 0, 0, 0, 0, 0},     {1, 1, 0, 0, 0, 0, 0, 0},     {1, 2, 1, 0, 0, 0, 0, 0},
+    {1, 3, 3, 1, 0, 0, 0, 0},     {1, 4, 6, 4, 1, 0, 0, 0},     {1, 5, 10, 10, 5, 1, 0, 0},
+    {1, 6, 15, 20, 15, 6, 1, 0},  {1, 7, 21, 35, 35, 21, 7, 1}};
+// the (x)-th subset of `mask`: the low bits of x deposited on mask's set bits
+__device__ __forceinline__ int deposit(int x, int mask) {
+    int r = 0;
+    for (int m = mask; m; m &= m - 1) {
+        if (x & 1) r |= m & -m;
+        x >>= 1;
     }
+    return r;
+}
+
+// Per-warp scratch of one treelet.
+struct TreeletSmem {
+    float lb[7][6];     // bounds of the treelet's leaves
+    float la[7];        // their areas (expansion candidates)
+    float area[128];
+    float copt[128];
+    unsigned char popt[128];
+    int leaves[7];
+    int nodes[6];
+};
+
+// One treelet, all 32 lanes of the warp.  Formation, subset areas and the
+// dynamic programme run across the lanes; every float result is produced by
+// the same operations in the same order as the sequential restatement:
+// unions merge a subset's leaves in index order, and the best split of a
+// subset is the first partition, in the enumeration p = (p - d) & s, with the
+// least cost (each lane scans its share of the partitions in that order, and
+// ties between lanes go to the earlier partition).  Bounds and costs read
+// once from memory are kept in shared memory and reused where the
+// sequential code reads them again.
+__device__ void treelet_warp(int root, float root_cost, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl,
+                             float *cost, TreeletSmem &sm, int lane) {
+    if (lane == 0) {
+        const NodeL r = load_node(btn, root);
+        sm.leaves[0] = child_ref(r, false);
+        sm.leaves[1] = child_ref(r, true);
+    }
+    __syncwarp();
+    if (lane < 2) {
+        ref_bound6(sm.leaves[lane], btn, btl, sm.lb[lane]);
+        sm.la[lane] = area6(sm.lb[lane]);
+    }
+    __syncwarp();
+    int nl = 2, nn = 0;
     while (nl < 7) {
-        int best = -1;
-        float best_a = -1.f;
-        for (int i = 0; i < nl; i++) {
-            if (leaves[i] < 0) continue;
-            float b[6];
-            ref_bound6(leaves[i], btn, btl, b);
-            float a = area6(b);
-            if (a > best_a) { best_a = a; best = i; }
+        // expand the internal leaf of largest area (first index on ties)
+        float a = -1.f;
+        int bi = 32;
+        if (lane < nl && sm.leaves[lane] >= 0 && sm.la[lane] > -1.f) { a = sm.la[lane]; bi = lane; }
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (oi < 32 && (bi == 32 || oa > a || (oa == a && oi < bi))) { a = oa; bi = oi; }
         }
-        if (best < 0) break;
-        int nd = leaves[best];
-        nodes[nn++] = nd;
-        const NodeL x = load_node(btn, nd);
-        leaves[best] = child_ref(x, false);
-        leaves[nl++] = child_ref(x, true);
+        bi = __shfl_sync(0xffffffffu, bi, 0);
+        if (bi == 32) break;
+        if (lane == 0) {
+            const int nd = sm.leaves[bi];
+            sm.nodes[nn] = nd;
+            const NodeL x = load_node(btn, nd);
+            sm.leaves[bi] = child_ref(x, false);
+            sm.leaves[nl] = child_ref(x, true);
+        }
+        __syncwarp();
+        if (lane < 2) {
+            const int slot = lane == 0 ? bi : nl;
+            ref_bound6(sm.leaves[slot], btn, btl, sm.lb[slot]);
+            sm.la[slot] = area6(sm.lb[slot]);
+        }
+        __syncwarp();
+        ++nn;
+        ++nl;
     }
     if (nl < 3) return;
     const int nsub = 1 << nl;
-    float lb[7][6];
-    for (int i = 0; i < nl; i++) ref_bound6(leaves[i], btn, btl, lb[i]);
-    float area[128], copt[128];
-    unsigned char popt[128];
-    for (int s = 1; s < nsub; s++) {
+    if (lane < nl) {
+        // ref_cost: the subtree cost of an internal node, Ct * area of a leaf
+        const int r = sm.leaves[lane];
+        sm.copt[1 << lane] = r >= 0 ? __ldcg(cost + r) : 1.0f * area6(sm.lb[lane]);
+    }
+    for (int s = lane + 1; s < nsub; s += 32) {
         float b[6];
         bool first = true;
         for (int i = 0; i < nl; i++) {
             if (!((s >> i) & 1)) continue;
-            if (first) { for (int a = 0; a < 6; ++a) b[a] = lb[i][a]; first = false; }
-            else merge6(b, lb[i]);
+            if (first) { for (int q = 0; q < 6; ++q) b[q] = sm.lb[i][q]; first = false; }
+            else merge6(b, sm.lb[i]);
         }
-        area[s] = area6(b);
+        sm.area[s] = area6(b);
     }
-    for (int i = 0; i < nl; i++) copt[1 << i] = ref_cost(leaves[i], cost, btl);
+    __syncwarp();
     for (int k = 2; k <= nl; k++) {
-        for (int s = 1; s < nsub; s++) {
-            if (__popc(s) != k) continue;
-            float bestc = FLT_MAX;
-            int bp = 0;
-            int d = (s - 1) & s;
-            int p = (-d) & s;
-            while (p != 0) {
-                float c = copt[p] + copt[s ^ p];
-                if (c < bestc) { bestc = c; bp = p; }
-                p = (p - d) & s;
+        const int cnt = kBinom7[nl][k];
+        const int nparts = (1 << (k - 1)) - 1;
+        int g = 1;   // lanes per subset
+        while (g < nparts && 2 * g * cnt <= 32) g *= 2;
+        for (int base = 0; base < cnt * g; base += 32) {
+            const int item = base + lane;
+            const bool valid = item < cnt * g;
+            const int m = item / g, jj = item % g;
+            const int s = valid ? kSubsets[kSubsetStart[k] + m] : 0;
+            const int d = (s - 1) & s;
+            float bc = FLT_MAX;
+            int bj = -1;
+            if (valid && g == 1) {
+                int j = 0;
+                for (int p = (-d) & s; p != 0; p = (p - d) & s, ++j) {
+                    const float c = sm.copt[p] + sm.copt[s ^ p];
+                    if (c < bc) { bc = c; bj = j; }
+                }
+            } else if (valid) {
+                for (int j = jj; j < nparts; j += g) {
+                    const int p = deposit(j + 1, d);
+                    const float c = sm.copt[p] + sm.copt[s ^ p];
+                    if (c < bc) { bc = c; bj = j; }
+                }
             }
-            copt[s] = 1.2f * area[s] + bestc;
-            popt[s] = (unsigned char)bp;
+            for (int o = 1; o < g; o <<= 1) {
+                const float oc = __shfl_xor_sync(0xffffffffu, bc, o);
+                const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+                if (oj >= 0 && (bj < 0 || oc < bc || (oc == bc && oj < bj))) { bc = oc; bj = oj; }
+            }
+            if (valid && jj == 0) {
+                sm.copt[s] = 1.2f * sm.area[s] + bc;
+                sm.popt[s] = (unsigned char)(bj >= 0 ? deposit(bj + 1, d) : 0);
+            }
         }
+        __syncwarp();
     }
     const int full = nsub - 1;
-    if (!(copt[full] < __ldcg(cost + root))) return;
-    int slots[7];
+    if (!(sm.copt[full] < root_cost)) return;
+    if (lane != 0) return;
+    // rebuild (one lane): internal slots are root + nodes[], reused in DFS
+    // order; a child is a treelet leaf -(i+1) or a slot index
+    int slot_node[7], kid[7][2];
     int ns = 0;
-    slots[ns++] = root;
-    for (int i = 0; i < nn; i++) slots[ns++] = nodes[i];
-    int used = 0;
-    int st_s[16], st_n[16], top = 0;
-    st_s[top] = full; st_n[top] = slots[used++]; top++;
+    slot_node[ns++] = root;
+    for (int i = 0; i < nn; i++) slot_node[ns++] = sm.nodes[i];
+    int used = 1;
+    int st_s[8], st_u[8], top = 0;
+    st_s[top] = full; st_u[top] = 0; top++;
     while (top) {
         top--;
-        int s = st_s[top], nd = st_n[top];
-        int ls = popt[s], rs = s ^ ls;
+        const int s = st_s[top], u = st_u[top], nd = slot_node[u];
+        const int ls = sm.popt[s];
+        const int subs[2] = {ls, s ^ ls};
         int refs[2];
-        int subs[2] = {ls, rs};
         for (int c = 0; c < 2; c++) {
             if (__popc(subs[c]) == 1) {
-                refs[c] = leaves[__ffs(subs[c]) - 1];
+                const int i = __ffs(subs[c]) - 1;
+                kid[u][c] = -(i + 1);
+                refs[c] = sm.leaves[i];
             } else {
-                refs[c] = slots[used++];
-                st_s[top] = subs[c]; st_n[top] = refs[c]; top++;
+                const int v = used++;
+                kid[u][c] = v;
+                refs[c] = slot_node[v];
+                st_s[top] = subs[c]; st_u[top] = v; top++;
             }
         }
         ptgpu_bvh_node &p = btn[nd];
@@ -711,45 +809,76 @@ __device__ void treelet_at(int root, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, f
         if (refs[0] < 0) btl[-refs[0] - 1].nParent = nd; else btn[refs[0]].nParent = nd;
         if (refs[1] < 0) btl[-refs[1] - 1].nParent = nd; else btn[refs[1]].nParent = nd;
     }
-    __threadfence();
-    for (int i = used - 1; i >= 0; i--) {
-        int nd = slots[i];
-        ptgpu_bvh_node &p = btn[nd];
-        const NodeL q = load_node(btn, nd);
-        int lr = q.min == q.nLeft ? -(q.nLeft + 1) : q.nLeft;
-        int rr = q.max == q.nRight ? -(q.nRight + 1) : q.nRight;
-        float b[6], c[6];
-        ref_bound6(lr, btn, btl, b);
-        ref_bound6(rr, btn, btl, c);
-        merge6(b, c);
+    // bounds and costs bottom-up (children have higher slot indices):
+    // union of left then right, cost Ci * area + left cost + right cost
+    float sb[7][6], sc[7];
+    for (int u = used - 1; u >= 0; u--) {
+        float b[6], cl, cr;
+        const int l = kid[u][0], r = kid[u][1];
+        const float *lbp = l < 0 ? sm.lb[-l - 1] : sb[l];
+        const float *rbp = r < 0 ? sm.lb[-r - 1] : sb[r];
+        cl = l < 0 ? sm.copt[1 << (-l - 1)] : sc[l];
+        cr = r < 0 ? sm.copt[1 << (-r - 1)] : sc[r];
+        for (int q = 0; q < 6; ++q) b[q] = lbp[q];
+        merge6(b, rbp);
+        for (int q = 0; q < 6; ++q) sb[u][q] = b[q];
+        sc[u] = 1.2f * area6(b) + cl + cr;
+        ptgpu_bvh_node &p = btn[slot_node[u]];
         p.bound.min_x = b[0]; p.bound.max_x = b[1]; p.bound.min_y = b[2];
         p.bound.max_y = b[3]; p.bound.min_z = b[4]; p.bound.max_z = b[5];
-        cost[nd] = 1.2f * area6(b) + ref_cost(lr, cost, btl) + ref_cost(rr, cost, btl);
-        __threadfence();
+        cost[slot_node[u]] = sc[u];
     }
+    __threadfence();
 }
 
-__global__ void __launch_bounds__(128) k_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n,
-                                                  int *counters, float *cost) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int node = btl[k].nParent;
-    while (node >= 0 && node < n - 1) {
-        __threadfence();
-        if (atomicAdd(&counters[node], 1) == 0) return;    // the second arrival goes on
-        __threadfence();
-        // all of node's subtree is final: compute its cost, then restructure
-        {
-            const NodeL p = load_node(btn, node);
-            int lr = p.min == p.nLeft ? -(p.nLeft + 1) : p.nLeft;
-            int rr = p.max == p.nRight ? -(p.nRight + 1) : p.nRight;
-            float b[6];
-            ref_bound6(node, btn, btl, b);
-            cost[node] = 1.2f * area6(b) + ref_cost(lr, cost, btl) + ref_cost(rr, cost, btl);
+// Bottom-up over the tree: each lane climbs from its leaf and the second
+// arrival at a node owns it.  The lanes of a warp that own a node in the same
+// round hand their treelets to the whole warp one after another.
+constexpr int kTreeletThreads = 128;
+__global__ void __launch_bounds__(kTreeletThreads) k_treelet(ptgpu_bvh_node *btn,
+                                                              ptgpu_bvh_node *btl, int n,
+                                                              int *counters, float *cost) {
+    __shared__ TreeletSmem s_tl[kTreeletThreads / 32];
+    TreeletSmem &sm = s_tl[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int node = k < n ? btl[k].nParent : -1;
+    bool active = node >= 0 && node < n - 1;
+    while (__any_sync(0xffffffffu, active)) {
+        bool mine = false;
+        float my_cost = 0.f;
+        if (active) {
+            __threadfence();
+            if (atomicAdd(&counters[node], 1) == 0) {
+                active = false;                    // the second arrival goes on
+            } else {
+                __threadfence();
+                // all of node's subtree is final: its cost first
+                const NodeL p = load_node(btn, node);
+                int lr = p.min == p.nLeft ? -(p.nLeft + 1) : p.nLeft;
+                int rr = p.max == p.nRight ? -(p.nRight + 1) : p.nRight;
+                float b[6];
+                ref_bound6(node, btn, btl, b);
+                my_cost = 1.2f * area6(b) + ref_cost(lr, cost, btl) + ref_cost(rr, cost, btl);
+                cost[node] = my_cost;
+                mine = true;
+            }
         }
-        treelet_at(node, btn, btl, cost);
-        if (node == 0) return;
-        node = load_node(btn, node).nParent;
+        unsigned m = __ballot_sync(0xffffffffu, mine);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const int root = __shfl_sync(0xffffffffu, node, src);
+            const float rc = __shfl_sync(0xffffffffu, my_cost, src);
+            treelet_warp(root, rc, btn, btl, cost, sm, lane);
+            __syncwarp();
+        }
+        if (mine) {
+            __threadfence();
+            if (node == 0) active = false;
+            else node = load_node(btn, node).nParent;
+            if (node < 0 || node >= n - 1) active = false;
+        }
     }
 }
 
@@ -769,7 +898,8 @@ cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int 
     k_treelet_prepare<<<(n + 255) / 256, 256, 0, s>>>(btn, n, counters);
     for (int it = 0; it < sweeps; ++it) {
         if (it > 0) cudaMemsetAsync(counters, 0, sizeof(int) * (size_t)(n - 1), s);
-        k_treelet<<<(n + 127) / 128, 128, 0, s>>>(btn, btl, n, counters, cost);
+        k_treelet<<<(n + kTreeletThreads - 1) / kTreeletThreads, kTreeletThreads, 0, s>>>(
+            btn, btl, n, counters, cost);
     }
     k_treelet_finish<<<(n + 255) / 256, 256, 0, s>>>(btn, n, cost);
     return cudaGetLastError();

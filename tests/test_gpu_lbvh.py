@@ -91,21 +91,26 @@ def test_lbvh_4m_properties(built_lib):
     assert ms > 0
 
 
-@pytest.mark.parametrize("case", ["ico4", "soup", "cornell", "odd"])
-def test_treelet_matches_oracle(case, built_lib, orc):
+@pytest.mark.parametrize("case,sweeps", [("ico4", 1), ("soup", 1), ("cornell", 1), ("odd", 1),
+                                         ("ico4", 3), ("soup", 2), ("odd", 3), ("tiny", 3),
+                                         ("ico6", 3)])
+def test_treelet_matches_oracle(case, sweeps, built_lib, orc):
     """GPU treelet restructuring == the oracle's sequential restatement, byte
-    for byte; the SAH cost drops; every leaf stays in the tree once."""
+    for byte, after one or several rounds; the SAH cost drops."""
     import ptgpu_pc_gb300 as pt
     shapes = {"ico4": lambda: scenes.icosphere_scene(level=4)[0],
+              "ico6": lambda: scenes.icosphere_scene(level=6)[0],
               "soup": lambda: scenes.triangle_soup(30000, seed=4),
               "cornell": lambda: scenes.cornell_spheres()[0],
-              "odd": lambda: scenes.triangle_soup(4097, seed=5)}[case]()
+              "odd": lambda: scenes.triangle_soup(4097, seed=5),
+              "tiny": lambda: scenes.triangle_soup(5, seed=6)}[case]()
+    flags = abi.FLAG_TREELET | (abi.treelet_sweeps(sweeps) if sweeps > 1 else 0)
     with pt.Context(8, 8) as ctx:
         ctx.set_shapes(shapes, 0)
-        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET)
+        ctx.build(abi.ACCEL_BVH, flags)
         g_btn, g_btl = ctx.get_bvh()
     _, btn, btl, _ = orc.build_bvh(shapes)
-    o_btn, o_btl = orc.treelet_optimize(btn, btl)
+    o_btn, o_btl = orc.treelet_optimize(btn, btl, sweeps)
     assert g_btl.tobytes() == o_btl.tobytes()
     assert g_btn.tobytes() == o_btn.tobytes()
     if len(shapes) > 2:

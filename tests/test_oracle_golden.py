@@ -139,3 +139,22 @@ def test_render_cornell_spheres(orc):
     assert col.tobytes() == z["colors"].tobytes()
     assert np.array_equal(pix, z["pixels"])
     assert np.array_equal(sd, z["seeds_out"])
+
+
+def test_treelet_rounds_lower_sah_and_keep_leaves(orc):
+    """Each treelet round keeps every leaf exactly once and never raises the
+    SAH cost; later rounds start from the tree the earlier ones left."""
+    from ptgpu_pc_gb300 import scenes
+    shapes = scenes.triangle_soup(3000, seed=31)
+    _, btn, btl, _ = orc.build_bvh(shapes)
+    costs = [orc.sah_cost(btn, btl)]
+    for k in (1, 2, 3):
+        b, l = orc.treelet_optimize(btn, btl, k)
+        costs.append(orc.sah_cost(b, l))
+        # leaf children of the internal nodes: every leaf once
+        kids = np.concatenate([b["nLeft"][b["min"] == b["nLeft"]], b["nRight"][b["max"] == b["nRight"]]])
+        assert np.array_equal(np.sort(kids), np.arange(len(shapes)))
+    assert costs[1] <= costs[0] and costs[2] <= costs[1] + 1e-9 and costs[3] <= costs[2] + 1e-9
+    b2, l2 = orc.treelet_optimize(*orc.treelet_optimize(btn, btl, 1), 1)
+    b3, l3 = orc.treelet_optimize(btn, btl, 2)
+    assert b2["nLeft"].tobytes() == b3["nLeft"].tobytes()
