@@ -1,13 +1,14 @@
 // lbvh.cu -- GPU LBVH build for the reference BVH layout (CLBVH + BVH.cl).
 //
 // Pipeline (reference mode, all on one stream):
-//   k_centroid_bounds   centroid min/max over all shapes (CLBVH.cpp:91-123)
+//   k_centroid_bounds   centroid min/max over all shapes (CLBVH.cpp:91-123),
+//                       and each shape's bound as an aligned 32-byte record
 //   k_morton            30-bit Morton keys (CLBVH.cpp:125-164)
 //   k_hist4             digit histograms of all four radix passes
 //   k_onesweep x4       stable LSD radix sort of ~key (== the descending
 //                       stable bubble sort, CLBVH.cpp:31-47), 8-bit digits,
-//                       warp-level ranking, decoupled look-back with a
-//                       bounded spin
+//                       warp-level ranking through shared lane masks,
+//                       decoupled look-back with a bounded spin
 //   k_tiles             per 1024-leaf tile: leaf records + every internal node
 //                       inside the tile, bounds by an in-shared-memory
 //                       bottom-up reduction, then a climb over the tiles for
@@ -117,13 +118,22 @@ __global__ void k_init_state(BuildState *st) {
     }
 }
 
+// Centroid bounds, and each shape's bound stored as one aligned 32-byte
+// record for the later kernels (the emission kernel gathers it in sorted
+// order: one sector per leaf instead of a 36-byte vertex triple).
 __global__ void __launch_bounds__(256) k_centroid_bounds(const float *__restrict__ verts,
                                                           const uint8_t *__restrict__ type,
-                                                          int all_tri, int n, BuildState *st) {
+                                                          int all_tri, int n, BuildState *st,
+                                                          float4 *__restrict__ aabbs) {
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
-        f3 p = shape_centroid(verts, i, tri);
+        float b[6];
+        shape_bound(verts, i, tri, b);
+        aabbs[2 * (size_t)i] = make_float4(b[0], b[1], b[2], b[3]);
+        aabbs[2 * (size_t)i + 1] = make_float4(b[4], b[5], 0.f, 0.f);
+        f3 p = tri ? mk3((b[0] + b[1]) / 2.0f, (b[2] + b[3]) / 2.0f, (b[4] + b[5]) / 2.0f)
+                   : shape_centroid(verts, i, false);
         float c[3] = {p.x, p.y, p.z};
         for (int a = 0; a < 3; ++a) {
             if (c[a] == c[a]) {          // NaN centroids never pass the reference's < / >
@@ -177,6 +187,7 @@ __device__ __forceinline__ uint32_t morton30(uint32_t a, uint32_t b, uint32_t c)
 // back to the start: the tail of the array, read last by k_centroid_bounds,
 // is still in L2 when this kernel starts.
 __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
+                                                 const float4 *__restrict__ aabbs,
                                                  const uint8_t *__restrict__ type, int all_tri,
                                                  int n, const BuildState *st,
                                                  uint32_t *__restrict__ keys) {
@@ -187,7 +198,13 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
         int i = blk * 256 + threadIdx.x;
         if (i >= n) continue;
         bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
-        f3 p = shape_centroid(verts, i, tri);
+        f3 p;
+        if (tri) {   // the triangle's centroid is its bound's centre
+            const float4 b0 = aabbs[2 * (size_t)i], b1 = aabbs[2 * (size_t)i + 1];
+            p = mk3((b0.x + b0.y) / 2.0f, (b0.z + b0.w) / 2.0f, (b1.x + b1.y) / 2.0f);
+        } else {
+            p = shape_centroid(verts, i, false);
+        }
         uint32_t qa = quantise10(p.x, lo[0], hi[0]);
         uint32_t qb = quantise10(p.y, lo[1], hi[1]);
         uint32_t qc = quantise10(p.z, lo[2], hi[2]);
@@ -251,12 +268,24 @@ constexpr int kSortItems = 15;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;
+#ifndef PTGPU_LOOKBACK
+#define PTGPU_LOOKBACK 8
+#endif
+constexpr int kLookback = PTGPU_LOOKBACK;   // predecessors read per look-back step
+#ifndef PTGPU_SORT_MINBLOCKS
+#define PTGPU_SORT_MINBLOCKS 3
+#endif
 
+// Look-back words are read and published with relaxed GPU-scope accesses:
+// each read sees the word as it is in L2, and several reads of one thread
+// can be in flight at once.
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
-    return *reinterpret_cast<const volatile uint32_t *>(p);
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
 __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) {
-    *reinterpret_cast<volatile uint32_t *>(p) = v;
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // block-wide exclusive scan of one value per thread (256 threads)
@@ -290,14 +319,22 @@ struct SortSmem {
     uint32_t digit_start[256];
     uint32_t tile_excl[256];
     uint32_t scan_tmp[32];
-    uint32_t keys[kSortTile];
-    int32_t vals[kSortTile];
+    union {
+        // ranking: per-warp lane masks of each digit, two sets used by
+        // alternate items so that clearing one never races with filling it
+        uint32_t match[2][kSortWarps][256];
+        // scatter: the tile in sorted order
+        struct {
+            uint32_t keys[kSortTile];
+            int32_t vals[kSortTile];
+        } st;
+    } u;
     int tile;
     int abort;
 };
 
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__restrict__ keys_in,
+__global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep(const uint32_t *__restrict__ keys_in,
                                                             const int32_t *__restrict__ vals_in,
                                                             uint32_t *__restrict__ keys_out,
                                                             int32_t *__restrict__ vals_out, int n,
@@ -309,6 +346,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__res
     const int shift = 8 * pass;
     if (tid == 0) { sm.tile = (int)atomicAdd(&st->tile_counter[pass], 1u); sm.abort = 0; }
     for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&sm.warp_hist[0][0])[i] = 0u;
+    for (int i = tid; i < 2 * kSortWarps * 256; i += kSortThreads) (&sm.u.match[0][0][0])[i] = 0u;
     // global digit offsets for this pass
     uint32_t gcount = st->hist[pass][tid];
     uint32_t goff = block_excl_scan256(gcount, sm.scan_tmp);
@@ -319,23 +357,37 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__res
     int32_t val[kSortItems];
     uint32_t rank[kSortItems];
     const unsigned lt_mask = (1u << lane) - 1u;
+    // all loads first: the ranking below synchronises the warp per item, and
+    // a load may not move across that
 #pragma unroll
     for (int j = 0; j < kSortItems; ++j) {
-        int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
-        bool valid = idx < n;
+        const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
+        const bool valid = idx < n;
         key[j] = valid ? keys_in[idx] : 0xffffffffu;
         val[j] = valid ? (FIRST ? (int32_t)idx : vals_in[idx]) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
+        const bool valid = idx < n;
         uint32_t dig = (key[j] >> shift) & 255u;
-        unsigned vm = __ballot_sync(0xffffffffu, valid);
+        // lanes with the same digit: each sets its bit in the digit's mask
+        uint32_t *mask = &sm.u.match[j & 1][w][dig];
+        if (valid) atomicOr(mask, 1u << lane);
+        __syncwarp();
         rank[j] = 0xffffffffu;
+        uint32_t prev = 0u;
+        unsigned peers = 0u;
         if (valid) {
-            unsigned peers = __match_any_sync(vm, dig);
-            uint32_t prev = sm.warp_hist[w][dig];
+            peers = *mask;
+            prev = sm.warp_hist[w][dig];
             rank[j] = prev + (uint32_t)__popc(peers & lt_mask);
-            __syncwarp(peers);
-            if (lane == __ffs(peers) - 1) sm.warp_hist[w][dig] = prev + (uint32_t)__popc(peers);
         }
         __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) {
+            sm.warp_hist[w][dig] = prev + (uint32_t)__popc(peers);
+            *mask = 0u;
+        }
     }
     __syncthreads();
     // per-digit counts: exclusive prefix over warps, tile total
@@ -355,21 +407,32 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__res
         st_volatile(my, kFlagInc | count);
     } else {
         st_volatile(my, kFlagAgg | count);
+        // the words of kLookback predecessors are read at once, then summed
+        // from the nearest back to the first inclusive one; a word not yet
+        // published ends the window and is read again
         int p = tile - 1;
         bool timed_out = false;
+        int spins = 0;
         while (p >= 0) {
-            uint32_t v;
-            int spins = 0;
-            for (;;) {
-                v = ld_volatile(status + (size_t)p * 256 + tid);
-                if (v & (3u << 30)) break;
+            uint32_t v[kLookback];
+#pragma unroll
+            for (int q = 0; q < kLookback; ++q)
+                v[q] = p - q >= 0 ? ld_volatile(status + (size_t)(p - q) * 256 + tid) : 0u;
+            int q = 0;
+            bool done = false;
+#pragma unroll
+            for (; q < kLookback; ++q) {
+                const uint32_t f = v[q] & (3u << 30);
+                if (f == 0u) break;
+                excl += v[q] & kValMask;
+                if (f == kFlagInc) { done = true; break; }
+            }
+            if (done) break;
+            p -= q;
+            if (q < kLookback) {
                 if (++spins > kSpinLimit) { timed_out = true; break; }
                 __nanosleep(32);
             }
-            if (timed_out) break;
-            excl += v & kValMask;
-            if ((v & (3u << 30)) == kFlagInc) break;
-            --p;
         }
         if (timed_out) { atomicOr(&st->error, 1u); sm.abort = 1; }
         st_volatile(my, kFlagInc | ((excl + count) & kValMask));
@@ -382,20 +445,20 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__res
         if (rank[j] != 0xffffffffu) {
             uint32_t dig = (key[j] >> shift) & 255u;
             uint32_t pos = sm.digit_start[dig] + sm.warp_hist[w][dig] + rank[j];
-            sm.keys[pos] = key[j];
-            sm.vals[pos] = val[j];
+            sm.u.st.keys[pos] = key[j];
+            sm.u.st.vals[pos] = val[j];
         }
     }
     __syncthreads();
     if (sm.abort) return;
     const int valid_cnt = (int)min((int64_t)kSortTile, (int64_t)n - base);
     for (int i = tid; i < valid_cnt; i += kSortThreads) {
-        uint32_t k = sm.keys[i];
+        uint32_t k = sm.u.st.keys[i];
         uint32_t dig = (k >> shift) & 255u;
         uint32_t dest = sm.tile_excl[dig] + ((uint32_t)i - sm.digit_start[dig]);
         if (dest < (uint32_t)n) {
             if (!LAST) keys_out[dest] = k;
-            vals_out[dest] = sm.vals[i];
+            vals_out[dest] = sm.u.st.vals[i];
         }
     }
 }
@@ -412,9 +475,12 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t *__res
 // bound goes to a per-level array, and of the two tiles (then blocks) under
 // a parent the one that arrives second merges them and moves up.
 // ---------------------------------------------------------------------------
-constexpr int kTileLeaves = 1024;
-constexpr int kTileLog = 10;
-constexpr int kTileThreads = 512;
+#ifndef PTGPU_TILE_LOG
+#define PTGPU_TILE_LOG 10
+#endif
+constexpr int kTileLog = PTGPU_TILE_LOG;
+constexpr int kTileLeaves = 1 << kTileLog;
+constexpr int kTileThreads = kTileLeaves / 2;   // two leaves per thread
 constexpr int kRecWords = 15;
 constexpr size_t kTileSmem = (6 * kTileLeaves) * sizeof(float) + kTileLeaves * kRecWords * 4 + kTileLeaves;
 
@@ -463,9 +529,8 @@ __device__ __forceinline__ int level_offset(int level, int ntiles) {
     return off;
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_tiles(const float *__restrict__ verts,
-                                                         const uint8_t *__restrict__ type,
-                                                         int all_tri, const int32_t *__restrict__ sorted,
+__global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict__ aabbs,
+                                                         const int32_t *__restrict__ sorted,
                                                          int n, ptgpu_bvh_node *__restrict__ btn,
                                                          ptgpu_bvh_node *__restrict__ btl,
                                                          float *__restrict__ block_bounds,
@@ -477,17 +542,37 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float *__restrict_
     const int T0 = blockIdx.x * kTileLeaves;
     const int cnt = min(kTileLeaves, n - T0);
     const int tid = threadIdx.x;
-    // ---- leaves
-    for (int k = tid; k < cnt; k += kTileThreads) {
-        const int leaf = T0 + k;
-        const int s = min(max(sorted[leaf], 0), n - 1);   // in bounds even after a failed sort
-        const bool tri = all_tri || type[s] == PTGPU_TRIANGLE;
-        float b[6];
-        shape_bound(verts, s, tri, b);
-        for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + k] = b[a];
-        const int parent = n >= 2 ? topo_parent_leaf(leaf, n) : -1;
-        stage_node(rec + k * kRecWords, -1, -1, s, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
-        own[k] = 0;
+    // ---- leaves: both of a thread's gathers are issued before either is used
+    {
+        int sh[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int k = tid + u * kTileThreads;
+            // in bounds even after a failed sort
+            sh[u] = k < cnt ? min(max(__ldg(sorted + T0 + k), 0), n - 1) : 0;
+        }
+        float4 q[2][2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            q[u][0] = __ldg(aabbs + 2 * (size_t)sh[u]);
+            q[u][1] = __ldg(aabbs + 2 * (size_t)sh[u] + 1);
+        }
+        float b[2][6];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            b[u][0] = q[u][0].x; b[u][1] = q[u][0].y; b[u][2] = q[u][0].z;
+            b[u][3] = q[u][0].w; b[u][4] = q[u][1].x; b[u][5] = q[u][1].y;
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int k = tid + u * kTileThreads;
+            if (k >= cnt) continue;
+            for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + k] = b[u][a];
+            const int parent = n >= 2 ? topo_parent_leaf(T0 + k, n) : -1;
+            stage_node(rec + k * kRecWords, -1, -1, sh[u], -1, -1, -1, parent, b[u], 0xffffffffu,
+                       0xffffffffu);
+            own[k] = 0;
+        }
     }
     __syncthreads();
     {
@@ -1056,6 +1141,9 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
         cudaFuncSetAttribute(k_onesweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_onesweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+        cudaFuncSetAttribute(k_onesweep<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(k_onesweep<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(k_onesweep<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
     k_init_state<<<1, 256, 0, s>>>(b.state);
@@ -1064,8 +1152,8 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
     e = cudaMemsetAsync(b.arrivals, 0, block_bound_count(n) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     const int red_grid = grid_for(n, 256, sm_count * 8);
-    k_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state);
-    k_morton<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state, b.keys);
+    k_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state, b.aabbs);
+    k_morton<<<red_grid, 256, 0, s>>>(b.verts, b.aabbs, b.type, all_tri, n, b.state, b.keys);
     k_hist4<<<grid_for((n + kHistItems - 1) / kHistItems, 256, sm_count * 4), 256, 0, s>>>(b.keys, n, b.state);
     const size_t pass_words = (size_t)ntiles_sort * 256;
     // pass 0: keys -> (keys_alt, vals_alt); 1: alt -> tmp; 2: tmp -> alt; 3: alt -> sorted
@@ -1077,8 +1165,8 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
         b.keys_tmp, b.vals_tmp, b.keys_alt, b.vals_alt, n, 2, b.state, b.status + 2 * pass_words);
     k_onesweep<false, true><<<ntiles_sort, kSortThreads, smem, s>>>(
         b.keys_alt, b.vals_alt, nullptr, b.sorted, n, 3, b.state, b.status + 3 * pass_words);
-    k_tiles<<<ntiles, kTileThreads, kTileSmem, s>>>(b.verts, b.type, all_tri, b.sorted, n, b.btn,
-                                                    b.btl, b.block_bounds, b.arrivals, ntiles);
+    k_tiles<<<ntiles, kTileThreads, kTileSmem, s>>>(b.aabbs, b.sorted, n, b.btn, b.btl,
+                                                    b.block_bounds, b.arrivals, ntiles);
     return cudaGetLastError();
 }
 

@@ -7,8 +7,8 @@
 // a plug-in host that forbids its plug-ins to allocate.  For them
 // ptgpu_build_bvh_noalloc builds the reference BVH (CLBVH.cpp: Morton codes,
 // radix sort, radix tree, refit) from shapes and into node arrays that the
-// caller has put in device memory.  Every intermediate -- vertices, Morton
-// keys, sort buffers, look-back words, block bounds -- lives in one
+// caller has put in device memory.  Every intermediate -- vertices, bounds,
+// Morton keys, sort buffers, look-back words, block bounds -- lives in one
 // file-scope __device__ array of fixed size, carved per call below.
 //
 // The array exists once per device the library is loaded on and is held until
@@ -32,9 +32,9 @@ int record_error(int code, const std::string &msg);
 
 namespace {
 
-// 16.3 MiB are needed at kNoAllocMaxShapes; the rest is slack
+// 24.3 MiB are needed at kNoAllocMaxShapes; the rest is slack
 constexpr uint32_t kNoAllocMaxShapes = 1u << 18;
-constexpr size_t kNoAllocScratchBytes = size_t(17) << 20;
+constexpr size_t kNoAllocScratchBytes = size_t(25) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -54,6 +54,7 @@ size_t carve(unsigned char *base, size_t n, LbvhBuffers &b) {
     };
     b.verts = reinterpret_cast<float *>(take(n * 9 * sizeof(float)));
     b.type = take(n);
+    b.aabbs = reinterpret_cast<float4 *>(take(n * 2 * sizeof(float4)));
     b.keys = reinterpret_cast<uint32_t *>(take(n * 4));
     b.keys_alt = reinterpret_cast<uint32_t *>(take(n * 4));
     b.keys_tmp = reinterpret_cast<uint32_t *>(take(n * 4));
