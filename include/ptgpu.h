@@ -206,6 +206,57 @@ int  ptgpu_trace_closest_device(ptgpu_ctx *ctx, const ptgpu_ray *d_rays,
                                 int32_t *d_hit);
 int  ptgpu_get_stream(ptgpu_ctx *ctx, void **stream);
 
+/* ---- batched scenes ------------------------------------------------------- */
+/* No counterpart in the reference (its process renders one scene).  A batch
+ * holds many scenes -- shapes, camera, image size, passes, seeds each -- and
+ * builds every scene's LBVH in one segmented pass of the build kernels (one
+ * radix sort over all scenes' keys), then renders all scenes' pixels in one
+ * persistent launch replayed from a CUDA graph.  A scene's BVH arrays,
+ * colours and pixels are the ones a single-scene context produces from the
+ * same inputs and build flags.  BVH only; binary traversal; up to 256 scenes
+ * of at least 2 shapes each.  One thread per batch.                          */
+typedef struct ptgpu_batch ptgpu_batch;
+
+typedef struct {
+    const ptgpu_shape *shapes;  /* n shapes, copied by ptgpu_batch_add           */
+    uint32_t n, light_cnt;      /* as ptgpu_set_shapes                          */
+    ptgpu_camera camera;        /* orig/pitch/yaw; UpdateCamera runs on add     */
+    int32_t width, height;
+    int32_t passes;             /* passes of one ptgpu_batch_render              */
+    int32_t max_depth;          /* 0 selects PTGPU_MAX_DEPTH                     */
+    const uint32_t *seeds;      /* 2*width*height seeds, copied                  */
+} ptgpu_scene;
+
+typedef struct {
+    float build_ms;             /* last ptgpu_batch_build: device time            */
+    float render_ms;            /* last ptgpu_batch_render: device time           */
+    double samples;             /* samples of one render (sum of W*H*passes)      */
+    int32_t block, refill, stack; /* launch settings in use (ptgpu_batch_tune)    */
+    int32_t tree_depth;         /* deepest leaf over all scenes' trees           */
+    int64_t shapes;             /* shapes over all scenes                         */
+} ptgpu_batch_info;
+
+int  ptgpu_batch_create(int32_t device, uint32_t flags, ptgpu_batch **out); /* flags: PTGPU_FLAG_ARGS_RTL */
+int  ptgpu_batch_destroy(ptgpu_batch *b);
+int  ptgpu_batch_add(ptgpu_batch *b, const ptgpu_scene *scene, int32_t *scene_id);
+/* Uploads every scene and builds all trees (build flags as ptgpu_build with
+ * PTGPU_ACCEL_BVH: PTGPU_FLAG_TREELET, PTGPU_TREELET_SWEEPS).  Resets the
+ * accumulation. */
+int  ptgpu_batch_build(ptgpu_batch *b, uint32_t flags);
+/* Times short one-pass renders of the batch over block sizes (64, 96, 128)
+ * and refill thresholds (16, 20, 24 of 32 lanes), keeps the fastest, and
+ * restores the seeds; the stack depth (32 or 64) follows the deepest tree.
+ * Resets the accumulation. */
+int  ptgpu_batch_tune(ptgpu_batch *b);
+/* One frame: each scene's `passes` passes, accumulated onto its running mean
+ * (the first frame after build/reset overwrites).  Returns when done. */
+int  ptgpu_batch_render(ptgpu_batch *b);
+int  ptgpu_batch_reset(ptgpu_batch *b);
+int  ptgpu_batch_get_pixels(ptgpu_batch *b, int32_t scene, uint32_t *pixels);   /* W*H RGBA8 */
+int  ptgpu_batch_get_colors(ptgpu_batch *b, int32_t scene, ptgpu_vec *colors);  /* W*H, row-flipped */
+int  ptgpu_batch_get_bvh(ptgpu_batch *b, int32_t scene, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl);
+int  ptgpu_batch_info_get(ptgpu_batch *b, ptgpu_batch_info *info);
+
 /* ---- BVH build without device allocation ----------------------------------- */
 /* No counterpart in the reference.  The LBVH build of ptgpu_build(ctx,
  * PTGPU_ACCEL_BVH, 0) -- same btn[n-1] / btl[n] bytes -- from n shapes in
@@ -249,6 +300,11 @@ PTGPU_SA(sizeof(ptgpu_bvh_node) == 60, "BVHNodeGPU is 60 bytes");
 PTGPU_SA(offsetof(ptgpu_bvh_node, bound) == 28, "BVHNodeGPU.bound at 28");
 PTGPU_SA(sizeof(ptgpu_kd_node) == 36, "KDNodeGPU is 36 bytes");
 PTGPU_SA(offsetof(ptgpu_kd_node, min) == 32, "KDNodeGPU.min at 32");
+/* the batch structs (no reference counterpart): fixed for foreign bindings */
+PTGPU_SA(sizeof(ptgpu_scene) == 120, "ptgpu_scene is 120 bytes");
+PTGPU_SA(offsetof(ptgpu_scene, camera) == 16, "ptgpu_scene.camera at 16");
+PTGPU_SA(offsetof(ptgpu_scene, seeds) == 112, "ptgpu_scene.seeds at 112");
+PTGPU_SA(sizeof(ptgpu_batch_info) == 40, "ptgpu_batch_info is 40 bytes");
 #undef PTGPU_SA
 
 #endif /* PTGPU_H */

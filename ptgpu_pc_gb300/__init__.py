@@ -26,6 +26,9 @@ EXPORTS = [
     "ptgpu_get_pixels", "ptgpu_get_current_sample", "ptgpu_trace_closest",
     "ptgpu_trace_closest_device", "ptgpu_get_stream", "ptgpu_render_stats",
     "ptgpu_build_bvh_noalloc",
+    "ptgpu_batch_create", "ptgpu_batch_destroy", "ptgpu_batch_add", "ptgpu_batch_build",
+    "ptgpu_batch_tune", "ptgpu_batch_render", "ptgpu_batch_reset", "ptgpu_batch_get_pixels",
+    "ptgpu_batch_get_colors", "ptgpu_batch_get_bvh", "ptgpu_batch_info_get",
 ]
 
 _lib = None
@@ -65,6 +68,17 @@ def lib():
         L.ptgpu_get_camera.argtypes = [vp, vp]
         L.ptgpu_build.argtypes = [vp, i32, u32]
         L.ptgpu_build_bvh_noalloc.argtypes = [vp, u32, vp, vp, vp]
+        L.ptgpu_batch_create.argtypes = [i32, u32, ctypes.POINTER(vp)]
+        L.ptgpu_batch_destroy.argtypes = [vp]
+        L.ptgpu_batch_add.argtypes = [vp, vp, ctypes.POINTER(i32)]
+        L.ptgpu_batch_build.argtypes = [vp, u32]
+        L.ptgpu_batch_tune.argtypes = [vp]
+        L.ptgpu_batch_render.argtypes = [vp]
+        L.ptgpu_batch_reset.argtypes = [vp]
+        L.ptgpu_batch_get_pixels.argtypes = [vp, i32, vp]
+        L.ptgpu_batch_get_colors.argtypes = [vp, i32, vp]
+        L.ptgpu_batch_get_bvh.argtypes = [vp, i32, vp, vp]
+        L.ptgpu_batch_info_get.argtypes = [vp, vp]
         L.ptgpu_get_bvh.argtypes = [vp, vp, vp]
         L.ptgpu_set_bvh.argtypes = [vp, vp, vp, u32]
         L.ptgpu_get_kdtree.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]
@@ -275,3 +289,83 @@ class Context:
         s = ctypes.c_void_p()
         _check(lib().ptgpu_get_stream(self._h, ctypes.byref(s)))
         return s.value or 0
+
+
+class Batch:
+    """Many scenes, one segmented LBVH build and one graph-replayed render
+    launch (ptgpu_batch_* in include/ptgpu.h)."""
+
+    def __init__(self, device=0, flags=0):
+        self._h = ctypes.c_void_p()
+        _check(lib().ptgpu_batch_create(device, flags, ctypes.byref(self._h)))
+        self._scenes = []
+
+    def add(self, shapes, light_cnt, camera, width, height, passes, seeds, max_depth=0):
+        """Adds a scene (copied); returns its id."""
+        shapes = abi.as_struct(shapes, abi.SHAPE)
+        seeds = np.ascontiguousarray(seeds, np.uint32)
+        if seeds.size != 2 * width * height:
+            raise ValueError("seeds must hold 2*width*height words")
+        d = np.zeros(1, abi.SCENE)
+        d["shapes"] = shapes.ctypes.data
+        d["n"], d["light_cnt"] = len(shapes), light_cnt
+        d["camera"] = np.array(camera, abi.CAMERA)
+        d["width"], d["height"], d["passes"], d["max_depth"] = width, height, passes, max_depth
+        d["seeds"] = seeds.ctypes.data
+        sid = ctypes.c_int32()
+        _check(lib().ptgpu_batch_add(self._h, d.ctypes.data, ctypes.byref(sid)))
+        self._scenes.append((width, height, len(shapes)))
+        return sid.value
+
+    def build(self, flags=0):
+        _check(lib().ptgpu_batch_build(self._h, flags))
+
+    def tune(self):
+        _check(lib().ptgpu_batch_tune(self._h))
+
+    def render(self):
+        _check(lib().ptgpu_batch_render(self._h))
+
+    def reset(self):
+        _check(lib().ptgpu_batch_reset(self._h))
+
+    def pixels(self, scene):
+        w, h, _ = self._scenes[scene]
+        out = np.zeros(w * h, np.uint32)
+        _check(lib().ptgpu_batch_get_pixels(self._h, scene, out.ctypes.data))
+        return out
+
+    def colors(self, scene):
+        w, h, _ = self._scenes[scene]
+        out = np.zeros((w * h, 3), np.float32)
+        _check(lib().ptgpu_batch_get_colors(self._h, scene, out.ctypes.data))
+        return out
+
+    def bvh(self, scene):
+        n = self._scenes[scene][2]
+        btn = np.zeros(n - 1, abi.BVH_NODE)
+        btl = np.zeros(n, abi.BVH_NODE)
+        _check(lib().ptgpu_batch_get_bvh(self._h, scene, btn.ctypes.data, btl.ctypes.data))
+        return btn, btl
+
+    def info(self):
+        out = np.zeros(1, abi.BATCH_INFO)
+        _check(lib().ptgpu_batch_info_get(self._h, out.ctypes.data))
+        return {k: out[k][0].item() for k in abi.BATCH_INFO.names}
+
+    def close(self):
+        if self._h:
+            lib().ptgpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

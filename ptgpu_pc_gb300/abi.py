@@ -56,6 +56,23 @@ CONFIG = np.dtype({
     "itemsize": 40,
 })
 
+# ptgpu_scene / ptgpu_batch_info (batched renders)
+SCENE = np.dtype({
+    "names": ["shapes", "n", "light_cnt", "camera", "width", "height", "passes", "max_depth",
+              "seeds"],
+    "formats": ["<u8", "<u4", "<u4", CAMERA, "<i4", "<i4", "<i4", "<i4", "<u8"],
+    "offsets": [0, 8, 12, 16, 92, 96, 100, 104, 112],
+    "itemsize": 120,
+})
+
+BATCH_INFO = np.dtype({
+    "names": ["build_ms", "render_ms", "samples", "block", "refill", "stack", "tree_depth",
+              "shapes"],
+    "formats": ["<f4", "<f4", "<f8", "<i4", "<i4", "<i4", "<i4", "<i8"],
+    "offsets": [0, 4, 8, 16, 20, 24, 28, 32],
+    "itemsize": 40,
+})
+
 # status codes (include/ptgpu.h)
 OK, E_INVAL, E_OOM, E_DEVICE, E_TIMEOUT, E_IO, E_RANGE, E_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 

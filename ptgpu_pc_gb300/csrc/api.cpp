@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 
+#include "devbuf.h"
 #include "host.h"
 #include "lbvh.h"
 
@@ -37,27 +38,6 @@ int cuda_fail(cudaError_t e, const char *what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #expr);        \
     } while (0)
 
-struct DevBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t want) {
-        if (want <= bytes && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        if (want == 0) want = 16;
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e == cudaSuccess) bytes = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
-};
-
 bool viszero(const ptgpu_vec &v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
 
 }  // namespace
@@ -65,6 +45,32 @@ bool viszero(const ptgpu_vec &v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f
 namespace ptgpu {
 // lets entry points outside this file report through ptgpu_last_error()
 int record_error(int code, const std::string &msg) { return fail(code, msg); }
+
+// SampleLights' emitters: the first light_cnt shapes with non-zero emission,
+// in index order
+void make_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
+                 std::vector<LightRec> &lights) {
+    lights.clear();
+    for (uint32_t i = 0; i < n && lights.size() < light_cnt; ++i) {
+        const ptgpu_shape &s = shapes[i];
+        if (viszero(s.e)) continue;
+        LightRec L;
+        std::memset(&L, 0, sizeof(L));
+        if (s.type == PTGPU_TRIANGLE) {
+            const ptgpu_triangle &t = s.g.t;
+            int32_t tt = PTGPU_TRIANGLE; float tf; std::memcpy(&tf, &tt, 4);
+            L.a = make_float4(t.p1.x, t.p1.y, t.p1.z, tf);
+            L.b = make_float4(t.p2.x - t.p1.x, t.p2.y - t.p1.y, t.p2.z - t.p1.z, s.area);
+            L.c = make_float4(t.p3.x - t.p1.x, t.p3.y - t.p1.y, t.p3.z - t.p1.z, 0.f);
+        } else {
+            int32_t tt = PTGPU_SPHERE; float tf; std::memcpy(&tf, &tt, 4);
+            L.a = make_float4(s.g.s.p.x, s.g.s.p.y, s.g.s.p.z, tf);
+            L.b = make_float4(s.g.s.rad, 0.f, 0.f, s.area);
+        }
+        L.e = make_float4(s.e.x, s.e.y, s.e.z, 0.f);
+        lights.push_back(L);
+    }
+}
 }  // namespace ptgpu
 
 struct ptgpu_ctx {
@@ -251,25 +257,7 @@ int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32
     for (uint32_t i = 0; i < n; ++i) if (shapes[i].type != PTGPU_TRIANGLE) { c->all_tri = false; break; }
     // emitters visited by SampleLights: the first light_cnt in index order
     std::vector<LightRec> lights;
-    for (uint32_t i = 0; i < n && lights.size() < light_cnt; ++i) {
-        const ptgpu_shape &s = shapes[i];
-        if (viszero(s.e)) continue;
-        LightRec L;
-        std::memset(&L, 0, sizeof(L));
-        if (s.type == PTGPU_TRIANGLE) {
-            const ptgpu_triangle &t = s.g.t;
-            int32_t tt = PTGPU_TRIANGLE; float tf; std::memcpy(&tf, &tt, 4);
-            L.a = make_float4(t.p1.x, t.p1.y, t.p1.z, tf);
-            L.b = make_float4(t.p2.x - t.p1.x, t.p2.y - t.p1.y, t.p2.z - t.p1.z, s.area);
-            L.c = make_float4(t.p3.x - t.p1.x, t.p3.y - t.p1.y, t.p3.z - t.p1.z, 0.f);
-        } else {
-            int32_t tt = PTGPU_SPHERE; float tf; std::memcpy(&tf, &tt, 4);
-            L.a = make_float4(s.g.s.p.x, s.g.s.p.y, s.g.s.p.z, tf);
-            L.b = make_float4(s.g.s.rad, 0.f, 0.f, s.area);
-        }
-        L.e = make_float4(s.e.x, s.e.y, s.e.z, 0.f);
-        lights.push_back(L);
-    }
+    make_lights(shapes, n, light_cnt, lights);
     c->n_lights = (int)lights.size();
     CK(c->d_shapes.ensure((size_t)n * sizeof(ptgpu_shape)));
     CK(c->d_verts.ensure((size_t)n * 9 * sizeof(float)));

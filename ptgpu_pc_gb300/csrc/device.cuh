@@ -174,13 +174,35 @@ struct Trav {
     int cur, ccnt; // current item: internal node (ccnt == 0) or leaf range
     int sp;
     int any, hit;  // shadow query; a hit was found (shadow: occluded)
+    int skip;      // shadow query: the shape id it never tests
 };
+
+// Where a query starts: the root item, the scene's shape count and the shape
+// IntersectP never tests (its last one).  A batched render keeps the nodes and
+// primitives of all its scenes in shared arrays and starts each query at its
+// scene's root.
+struct TraceRoot {
+    int32_t first, count;   // internal node `first` (count 0) or a leaf range
+    int32_t n_shapes;
+    int32_t skip;           // prim_id value of the scene's last shape
+    const float *box;       // min_x,max_x,min_y,max_y,min_z,max_z of the root
+};
+
+__device__ __forceinline__ TraceRoot view_root(const TraceView &tv) {
+    TraceRoot r;
+    r.first = tv.root_count > 0 ? tv.root_first : 0;
+    r.count = tv.root_count > 0 ? tv.root_count : 0;
+    r.n_shapes = tv.n_shapes;
+    r.skip = tv.n_shapes - 1;
+    r.box = tv.root_box;
+    return r;
+}
 
 // Starts a query.  Returns true when it is already answered (empty scene,
 // brute-force mode, or the root box missed).
 template <bool COUNT>
-__device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f3 d, bool any,
-                                           float maxt, Counts *cnt) {
+__device__ __forceinline__ bool trav_begin(const TraceView &tv, const TraceRoot &root, Trav &q,
+                                           f3 o, f3 d, bool any, float maxt, Counts *cnt) {
     q.o = o;
     q.d = d;
     q.any = any;
@@ -188,7 +210,8 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f
     q.prim = -1;
     q.tb = any ? maxt : kInfT;
     q.sp = 0;
-    const int n = tv.n_shapes;
+    q.skip = root.skip;
+    const int n = root.n_shapes;
     if (n <= 0 || (any && n <= 1)) return true;
     if (tv.accel == PTGPU_ACCEL_NONE) {
         if (any) {
@@ -209,13 +232,18 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f
     }
     q.inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
     float tmin, tmax;
-    if (!slab(__ldg(tv.root_box + 0), __ldg(tv.root_box + 1), __ldg(tv.root_box + 2),
-              __ldg(tv.root_box + 3), __ldg(tv.root_box + 4), __ldg(tv.root_box + 5), o, q.inv, tmin,
-              tmax))
+    if (!slab(__ldg(root.box + 0), __ldg(root.box + 1), __ldg(root.box + 2), __ldg(root.box + 3),
+              __ldg(root.box + 4), __ldg(root.box + 5), o, q.inv, tmin, tmax))
         return true;
-    q.cur = tv.root_count > 0 ? tv.root_first : 0;
-    q.ccnt = tv.root_count > 0 ? tv.root_count : 0;
+    q.cur = root.first;
+    q.ccnt = root.count;
     return false;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f3 d, bool any,
+                                           float maxt, Counts *cnt) {
+    return trav_begin<COUNT>(tv, view_root(tv), q, o, d, any, maxt, cnt);
 }
 
 // One item of the traversal: a leaf range's primitives or one node's
@@ -223,12 +251,11 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f
 #ifndef PTGPU_TRAV_FUSE
 #define PTGPU_TRAV_FUSE 1
 #endif
-template <bool WIDE, bool COUNT>
+template <bool WIDE, bool COUNT, int STACK = kStackSize>
 __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *stack, Counts *cnt) {
     if (q.ccnt > 0) {
-        const int skip = tv.n_shapes - 1;
         for (int k = q.cur; k < q.cur + q.ccnt; ++k) {
-            if (q.any && __ldg(&tv.prim_id[k]) == skip) continue;
+            if (q.any && __ldg(&tv.prim_id[k]) == q.skip) continue;
             float dd = prim_intersect(tv.prims, k, q.o, q.d);
             if (COUNT) cnt->p++;
             if (dd != 0.f) {
@@ -284,12 +311,12 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
             }
         }
         for (int a = ni - 1; a >= 0; --a) {
-            if (q.sp < kStackSize) stack[q.sp++] = iref[a];
+            if (q.sp < STACK) stack[q.sp++] = iref[a];
             else if (tv.error_flags) atomicOr(tv.error_flags, 1);
         }
         // leaves go on the stack as negative entries, tested before the nodes
         for (int a = nl - 1; a >= 0; --a) {
-            if (q.sp + 1 < kStackSize) { stack[q.sp++] = lcnt[a]; stack[q.sp++] = ~lref[a]; }
+            if (q.sp + 1 < STACK) { stack[q.sp++] = lcnt[a]; stack[q.sp++] = ~lref[a]; }
             else if (tv.error_flags) atomicOr(tv.error_flags, 1);
         }
     } else {
@@ -307,7 +334,7 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
             bool lfirst = !(rt0 < lt0);
             int fr = lfirst ? q3.y : q3.x, fc = lfirst ? q3.w : q3.z;
             int nr = lfirst ? q3.x : q3.y, nc = lfirst ? q3.z : q3.w;
-            if (q.sp + 1 < kStackSize) {
+            if (q.sp + 1 < STACK) {
                 if (fc > 0) { stack[q.sp++] = fc; stack[q.sp++] = ~fr; }
                 else stack[q.sp++] = fr;
             } else if (tv.error_flags) atomicOr(tv.error_flags, 1);

@@ -105,8 +105,8 @@ __host__ __device__ __forceinline__ float ord2f(uint32_t u) {
 
 __global__ void k_init_state(BuildState *st) {
     int t = threadIdx.x;
-    for (int i = t; i < 4 * 256; i += blockDim.x) (&st->hist[0][0])[i] = 0u;
-    if (t < 4) st->tile_counter[t] = 0u;
+    for (int i = t; i < 5 * 256; i += blockDim.x) (&st->hist[0][0])[i] = 0u;
+    if (t < 5) st->tile_counter[t] = 0u;
     if (t == 0) {
         st->error = 0u;
         st->top_ticket = 0u;
@@ -259,6 +259,121 @@ __global__ void __launch_bounds__(256) k_hist4(const uint32_t *__restrict__ keys
     }
 }
 
+// the segment holding shape v: the last s with off[s] <= v
+__device__ __forceinline__ uint32_t segment_of(const int32_t *off, int n_segs, int32_t v) {
+    int lo = 0, hi = n_segs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= v) lo = mid; else hi = mid - 1;
+    }
+    return (uint32_t)lo;
+}
+
+// ---------------------------------------------------------------------------
+// segmented build: per-segment centroid bounds and Morton keys
+// ---------------------------------------------------------------------------
+__global__ void k_seg_init(SegState *ss, int n_segs, BuildState *st, const int32_t *seg_off) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_segs) return;
+    for (int a = 0; a < 3; ++a) {
+        ss[g].cmin[a] = f2ord(FLT_MAX);
+        ss[g].cmax[a] = f2ord(FLT_MIN);
+    }
+    // the segment pass counts every shape of a segment under its digit
+    st->hist[4][g] = (uint32_t)(seg_off[g + 1] - seg_off[g]);
+}
+
+// Same per-shape work as k_centroid_bounds; the min/max go to the shape's
+// segment (one set of atomics per warp when the warp lies in one segment).
+__global__ void __launch_bounds__(256) k_seg_centroid_bounds(const float *__restrict__ verts,
+                                                              const uint8_t *__restrict__ type,
+                                                              int n, SegBuild sb,
+                                                              float4 *__restrict__ aabbs) {
+    __shared__ int32_t s_off[kMaxSegments + 1];
+    for (int i = threadIdx.x; i <= sb.n_segs; i += blockDim.x) s_off[i] = sb.seg_off[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // every lane of a warp runs the same number of rounds
+    const int64_t rounds = ((int64_t)n + stride - 1) / stride;
+    for (int64_t r = 0; r < rounds; ++r) {
+        const int64_t i = start + r * stride;
+        const bool valid = i < n;
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        int g = 0;
+        if (valid) {
+            g = (int)segment_of(s_off, sb.n_segs, (int32_t)i);
+            const bool tri = type[i] == PTGPU_TRIANGLE;
+            float b[6];
+            shape_bound(verts, (int)i, tri, b);
+            aabbs[2 * i] = make_float4(b[0], b[1], b[2], b[3]);
+            aabbs[2 * i + 1] = make_float4(b[4], b[5], 0.f, 0.f);
+            const f3 p = tri ? mk3((b[0] + b[1]) / 2.0f, (b[2] + b[3]) / 2.0f, (b[4] + b[5]) / 2.0f)
+                             : shape_centroid(verts, (int)i, false);
+            const float c[3] = {p.x, p.y, p.z};
+            for (int a = 0; a < 3; ++a)
+                if (c[a] == c[a]) { lo[a] = c[a]; hi[a] = c[a]; }   // NaN never counts
+        }
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        const int g0 = __shfl_sync(0xffffffffu, g, __ffs(vm | 1u) - 1);
+        const bool one = __all_sync(0xffffffffu, !valid || g == g0);
+        if (one) {
+            for (int a = 0; a < 3; ++a) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                    hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+                }
+            }
+            if (lane == 0 && vm) {
+                for (int a = 0; a < 3; ++a) {
+                    if (lo[a] <= hi[a]) {
+                        atomicMin(&sb.seg_state[g0].cmin[a], f2ord(lo[a]));
+                        atomicMax(&sb.seg_state[g0].cmax[a], f2ord(hi[a]));
+                    }
+                }
+            }
+        } else if (valid) {
+            for (int a = 0; a < 3; ++a) {
+                if (lo[a] <= hi[a]) {
+                    atomicMin(&sb.seg_state[g].cmin[a], f2ord(lo[a]));
+                    atomicMax(&sb.seg_state[g].cmax[a], f2ord(hi[a]));
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_seg_morton(const float *__restrict__ verts,
+                                                     const float4 *__restrict__ aabbs,
+                                                     const uint8_t *__restrict__ type, int n,
+                                                     SegBuild sb, uint32_t *__restrict__ keys) {
+    __shared__ int32_t s_off[kMaxSegments + 1];
+    for (int i = threadIdx.x; i <= sb.n_segs; i += blockDim.x) s_off[i] = sb.seg_off[i];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)segment_of(s_off, sb.n_segs, (int32_t)i);
+        float lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = ord2f(__ldg(&sb.seg_state[g].cmin[a]));
+            hi[a] = ord2f(__ldg(&sb.seg_state[g].cmax[a]));
+        }
+        const bool tri = type[i] == PTGPU_TRIANGLE;
+        f3 p;
+        if (tri) {
+            const float4 b0 = aabbs[2 * i], b1 = aabbs[2 * i + 1];
+            p = mk3((b0.x + b0.y) / 2.0f, (b0.z + b0.w) / 2.0f, (b1.x + b1.y) / 2.0f);
+        } else {
+            p = shape_centroid(verts, (int)i, false);
+        }
+        const uint32_t qa = quantise10(p.x, lo[0], hi[0]);
+        const uint32_t qb = quantise10(p.y, lo[1], hi[1]);
+        const uint32_t qc = quantise10(p.z, lo[2], hi[2]);
+        keys[i] = ~morton30(qa & 1023u, qb & 1023u, qc & 1023u);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // onesweep radix pass
 // ---------------------------------------------------------------------------
@@ -329,22 +444,31 @@ struct SortSmem {
             int32_t vals[kSortTile];
         } st;
     } u;
+    int32_t seg_off[kMaxSegments + 1];   // SEG: the segments' first shapes
     int tile;
     int abort;
 };
 
-template <bool FIRST, bool LAST>
+// One pass: stable counting sort of (key, val) by the 8-bit digit of key at
+// 8 * pass.  SEG (the last pass of a segmented build): the digit is the
+// segment of the value (a shape id), so the pass regroups the shapes by
+// segment and keeps each segment's key order.
+template <bool FIRST, bool LAST, bool SEG = false>
 __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep(const uint32_t *__restrict__ keys_in,
                                                             const int32_t *__restrict__ vals_in,
                                                             uint32_t *__restrict__ keys_out,
                                                             int32_t *__restrict__ vals_out, int n,
                                                             int pass, BuildState *st,
-                                                            uint32_t *status) {
+                                                            uint32_t *status,
+                                                            const int32_t *__restrict__ seg_off = nullptr,
+                                                            int n_segs = 0) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int shift = 8 * pass;
+    const int shift = SEG ? 0 : 8 * pass;
     if (tid == 0) { sm.tile = (int)atomicAdd(&st->tile_counter[pass], 1u); sm.abort = 0; }
+    if (SEG)
+        for (int i = tid; i <= n_segs; i += kSortThreads) sm.seg_off[i] = seg_off[i];
     for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&sm.warp_hist[0][0])[i] = 0u;
     for (int i = tid; i < 2 * kSortWarps * 256; i += kSortThreads) (&sm.u.match[0][0][0])[i] = 0u;
     // global digit offsets for this pass
@@ -363,8 +487,13 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     for (int j = 0; j < kSortItems; ++j) {
         const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
         const bool valid = idx < n;
-        key[j] = valid ? keys_in[idx] : 0xffffffffu;
         val[j] = valid ? (FIRST ? (int32_t)idx : vals_in[idx]) : -1;
+        if (!SEG) key[j] = valid ? keys_in[idx] : 0xffffffffu;
+    }
+    if (SEG) {   // seg_off is in shared memory after the barrier above
+#pragma unroll
+        for (int j = 0; j < kSortItems; ++j)
+            key[j] = val[j] >= 0 ? segment_of(sm.seg_off, n_segs, val[j]) : 0xffffffffu;
     }
 #pragma unroll
     for (int j = 0; j < kSortItems; ++j) {
@@ -529,17 +658,21 @@ __device__ __forceinline__ int level_offset(int level, int ntiles) {
     return off;
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict__ aabbs,
-                                                         const int32_t *__restrict__ sorted,
-                                                         int n, ptgpu_bvh_node *__restrict__ btn,
-                                                         ptgpu_bvh_node *__restrict__ btl,
-                                                         float *__restrict__ block_bounds,
-                                                         uint32_t *__restrict__ arrivals, int ntiles) {
-    extern __shared__ __align__(16) unsigned char tsm[];
+// One tile of one tree: `tile` counts the tree's tiles, `sorted` is the
+// tree's part of the sorted shape ids, whose values start at shape_base (the
+// leaves' nShape is the id minus shape_base); btn/btl/block_bounds/arrivals
+// are the tree's own arrays.
+__device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ aabbs,
+                                          const int32_t *__restrict__ sorted, int shape_base, int n,
+                                          ptgpu_bvh_node *__restrict__ btn,
+                                          ptgpu_bvh_node *__restrict__ btl,
+                                          float *__restrict__ block_bounds,
+                                          uint32_t *__restrict__ arrivals, int ntiles,
+                                          unsigned char *tsm) {
     float *sb = reinterpret_cast<float *>(tsm);                          // [6][1024]
     uint32_t *rec = reinterpret_cast<uint32_t *>(sb + 6 * kTileLeaves);  // [1024][15]
     unsigned char *own = reinterpret_cast<unsigned char *>(rec + kTileLeaves * kRecWords);
-    const int T0 = blockIdx.x * kTileLeaves;
+    const int T0 = tile * kTileLeaves;
     const int cnt = min(kTileLeaves, n - T0);
     const int tid = threadIdx.x;
     // ---- leaves: both of a thread's gathers are issued before either is used
@@ -549,7 +682,8 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict
         for (int u = 0; u < 2; ++u) {
             const int k = tid + u * kTileThreads;
             // in bounds even after a failed sort
-            sh[u] = k < cnt ? min(max(__ldg(sorted + T0 + k), 0), n - 1) : 0;
+            sh[u] = k < cnt ? min(max(__ldg(sorted + T0 + k) - shape_base, 0), n - 1) + shape_base
+                            : shape_base;
         }
         float4 q[2][2];
 #pragma unroll
@@ -569,7 +703,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict
             if (k >= cnt) continue;
             for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + k] = b[u][a];
             const int parent = n >= 2 ? topo_parent_leaf(T0 + k, n) : -1;
-            stage_node(rec + k * kRecWords, -1, -1, sh[u], -1, -1, -1, parent, b[u], 0xffffffffu,
+            stage_node(rec + k * kRecWords, -1, -1, sh[u] - shape_base, -1, -1, -1, parent, b[u], 0xffffffffu,
                        0xffffffffu);
             own[k] = 0;
         }
@@ -612,7 +746,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict
     float b[6];
     for (int a = 0; a < 6; ++a) b[a] = sb[a * kTileLeaves];
     int level = kTileLog;
-    int j = blockIdx.x;                                    // block index at `level`
+    int j = tile;                                          // block index at `level`
     int off = 0;                                           // level_offset(level)
     for (;;) {
         float *mine = block_bounds + 6 * (size_t)(off + j);
@@ -643,6 +777,33 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict
         j = pj;
         off = noff;
     }
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict__ aabbs,
+                                                         const int32_t *__restrict__ sorted,
+                                                         int n, ptgpu_bvh_node *__restrict__ btn,
+                                                         ptgpu_bvh_node *__restrict__ btl,
+                                                         float *__restrict__ block_bounds,
+                                                         uint32_t *__restrict__ arrivals, int ntiles) {
+    extern __shared__ __align__(16) unsigned char tsm[];
+    emit_tile(blockIdx.x, aabbs, sorted, 0, n, btn, btl, block_bounds, arrivals, ntiles, tsm);
+}
+
+// the tiles of every segment's tree in one launch
+__global__ void __launch_bounds__(kTileThreads) k_tiles_seg(const float4 *__restrict__ aabbs,
+                                                             const int32_t *__restrict__ sorted,
+                                                             SegBuild sb, ptgpu_bvh_node *__restrict__ btn,
+                                                             ptgpu_bvh_node *__restrict__ btl,
+                                                             float *__restrict__ block_bounds,
+                                                             uint32_t *__restrict__ arrivals) {
+    extern __shared__ __align__(16) unsigned char tsm[];
+    const int t = blockIdx.x;
+    const int g = (int)segment_of(sb.tile_off, sb.n_segs, t);
+    const int off = sb.seg_off[g], n = sb.seg_off[g + 1] - off;
+    const int tile = t - sb.tile_off[g];
+    const int64_t bb = sb.bb_off[g];
+    emit_tile(tile, aabbs, sorted + off, off, n, btn + (off - g), btl + off, block_bounds + 6 * bb,
+              arrivals + bb, sb.tile_off[g + 1] - sb.tile_off[g], tsm);
 }
 
 // ---------------------------------------------------------------------------
@@ -998,11 +1159,12 @@ cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int 
 __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
                                const ptgpu_bvh_node *__restrict__ btl, int n,
                                const float4 *__restrict__ prims0, float4 *__restrict__ nodes,
-                               float4 *__restrict__ prims, int32_t *__restrict__ prim_id) {
+                               float4 *__restrict__ prims, int32_t *__restrict__ prim_id,
+                               int node_base, int shape_base) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         int s = min(max(btl[i].nShape, 0), n - 1);
-        prim_id[i] = s;
+        prim_id[i] = shape_base + s;
         prims[3 * (size_t)i + 0] = prims0[3 * (size_t)s + 0];
         prims[3 * (size_t)i + 1] = prims0[3 * (size_t)s + 1];
         prims[3 * (size_t)i + 2] = prims0[3 * (size_t)s + 2];
@@ -1018,7 +1180,8 @@ __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
         o[0] = make_float4(lb.min_x, lb.max_x, lb.min_y, lb.max_y);
         o[1] = make_float4(lb.min_z, lb.max_z, rb.min_x, rb.max_x);
         o[2] = make_float4(rb.min_y, rb.max_y, rb.min_z, rb.max_z);
-        int4 q = make_int4(li, ri, ll ? 1 : 0, rl ? 1 : 0);
+        int4 q = make_int4((ll ? shape_base : node_base) + li, (rl ? shape_base : node_base) + ri,
+                           ll ? 1 : 0, rl ? 1 : 0);
         o[3] = *reinterpret_cast<float4 *>(&q);
     }
 }
@@ -1117,7 +1280,7 @@ cudaError_t launch_unpack_shapes(const ptgpu_shape *d_shapes, int n, float *vert
 
 size_t sort_status_words(int n) {
     size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
-    return tiles * 256 * 4;
+    return tiles * 256 * 5;
 }
 
 size_t block_bound_count(int n) {
@@ -1125,27 +1288,37 @@ size_t block_bound_count(int n) {
     return 2 * ntiles + 64;
 }
 
+template <class K> static void sort_attrs(K k, size_t smem) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
+// shared-memory opt-ins of the build kernels, once per device
+static cudaError_t launch_lbvh_prepare_attrs() {
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64 && attr_set[dev]) return cudaSuccess;
+    const size_t smem = sizeof(SortSmem);
+    sort_attrs(k_onesweep<true, false>, smem);
+    sort_attrs(k_onesweep<false, false>, smem);
+    sort_attrs(k_onesweep<false, true>, smem);
+    sort_attrs(k_onesweep<false, true, true>, smem);
+    cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+    cudaFuncSetAttribute(k_tiles_seg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+    if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_count,
                               cudaStream_t s) {
     if (n < 1) return cudaErrorInvalidValue;
     const int ntiles_sort = (n + kSortTile - 1) / kSortTile;
     const int ntiles = (n + kTileLeaves - 1) / kTileLeaves;
-    cudaError_t e;
-    // shared-memory opt-ins are per device
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
+    cudaError_t e = launch_lbvh_prepare_attrs();
+    if (e != cudaSuccess) return e;
     const size_t smem = sizeof(SortSmem);
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        cudaFuncSetAttribute(k_onesweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_onesweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_onesweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
-        cudaFuncSetAttribute(k_onesweep<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(k_onesweep<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(k_onesweep<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        if (dev >= 0 && dev < 64) attr_set[dev] = true;
-    }
     k_init_state<<<1, 256, 0, s>>>(b.state);
     e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
@@ -1170,11 +1343,53 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
     return cudaGetLastError();
 }
 
+size_t seg_block_bound_count(int n) { return block_bound_count(n); }
+int emission_tiles(int n) { return (n + kTileLeaves - 1) / kTileLeaves; }
+
+// The batched build: keys per segment, one radix sort of all keys (four key
+// passes, then the segment pass that regroups the shapes by segment while
+// keeping each segment's key order -- the order a separate sort of each
+// segment gives), and every segment's tiles in one launch.
+cudaError_t launch_lbvh_build_seg(const LbvhBuffers &b, int n, const SegBuild &sb, int sm_count,
+                                  cudaStream_t s) {
+    if (n < 2 || sb.n_segs < 1 || sb.n_segs > kMaxSegments) return cudaErrorInvalidValue;
+    cudaError_t e = launch_lbvh_prepare_attrs();
+    if (e != cudaSuccess) return e;
+    const int ntiles_sort = (n + kSortTile - 1) / kSortTile;
+    const size_t smem = sizeof(SortSmem);
+    k_init_state<<<1, 256, 0, s>>>(b.state);
+    k_seg_init<<<(sb.n_segs + 127) / 128, 128, 0, s>>>(sb.seg_state, sb.n_segs, b.state, sb.seg_off);
+    e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(b.arrivals, 0, (size_t)sb.n_blocks * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const int red_grid = grid_for(n, 256, sm_count * 8);
+    k_seg_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, n, sb, b.aabbs);
+    k_seg_morton<<<red_grid, 256, 0, s>>>(b.verts, b.aabbs, b.type, n, sb, b.keys);
+    k_hist4<<<grid_for((n + kHistItems - 1) / kHistItems, 256, sm_count * 4), 256, 0, s>>>(b.keys, n, b.state);
+    const size_t pw = (size_t)ntiles_sort * 256;
+    // keys -> alt -> tmp -> alt -> tmp, then the segment pass tmp -> sorted
+    k_onesweep<true, false><<<ntiles_sort, kSortThreads, smem, s>>>(
+        b.keys, nullptr, b.keys_alt, b.vals_alt, n, 0, b.state, b.status);
+    k_onesweep<false, false><<<ntiles_sort, kSortThreads, smem, s>>>(
+        b.keys_alt, b.vals_alt, b.keys_tmp, b.vals_tmp, n, 1, b.state, b.status + pw);
+    k_onesweep<false, false><<<ntiles_sort, kSortThreads, smem, s>>>(
+        b.keys_tmp, b.vals_tmp, b.keys_alt, b.vals_alt, n, 2, b.state, b.status + 2 * pw);
+    k_onesweep<false, false><<<ntiles_sort, kSortThreads, smem, s>>>(
+        b.keys_alt, b.vals_alt, b.keys_tmp, b.vals_tmp, n, 3, b.state, b.status + 3 * pw);
+    k_onesweep<false, true, true><<<ntiles_sort, kSortThreads, smem, s>>>(
+        nullptr, b.vals_tmp, nullptr, b.sorted, n, 4, b.state, b.status + 4 * pw, sb.seg_off, sb.n_segs);
+    k_tiles_seg<<<sb.n_tiles, kTileThreads, kTileSmem, s>>>(b.aabbs, b.sorted, sb, b.btn, b.btl,
+                                                            b.block_bounds, b.arrivals);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_abi_to_trace(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, int n,
                                 const float4 *prims0, float4 *nodes, float4 *prims,
-                                int32_t *prim_id, cudaStream_t s) {
+                                int32_t *prim_id, cudaStream_t s, int node_base, int shape_base) {
     if (n <= 0) return cudaSuccess;
-    k_abi_to_trace<<<(n + 255) / 256, 256, 0, s>>>(btn, btl, n, prims0, nodes, prims, prim_id);
+    k_abi_to_trace<<<(n + 255) / 256, 256, 0, s>>>(btn, btl, n, prims0, nodes, prims, prim_id,
+                                                    node_base, shape_base);
     return cudaGetLastError();
 }
 

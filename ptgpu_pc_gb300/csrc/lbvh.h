@@ -3,6 +3,8 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../../include/ptgpu.h"
@@ -12,8 +14,9 @@ namespace ptgpu {
 
 // Per-build device state, zeroed by the first kernel of every build.
 struct BuildState {
-    uint32_t hist[4][256];      // digit histograms of the four radix passes
-    uint32_t tile_counter[4];   // dynamic tile ids of the onesweep passes
+    uint32_t hist[5][256];      // digit histograms of the radix passes (the fifth:
+                                // the segment pass of a batched build)
+    uint32_t tile_counter[5];   // dynamic tile ids of the onesweep passes
     uint32_t cmin[3], cmax[3];  // centroid bounds as order-preserving uints
     uint32_t error;             // bit 0: a look-back wait gave up
     uint32_t top_ticket;
@@ -34,18 +37,41 @@ struct LbvhBuffers {
     ptgpu_bvh_node *btn, *btl;  // the reference's output arrays
 };
 
-size_t sort_status_words(int n);
+size_t sort_status_words(int n);   // look-back words of all (five) passes
 size_t block_bound_count(int n);   // blocks at the tile level and above (+ slack)
 
 cudaError_t launch_unpack_shapes(const ptgpu_shape *d_shapes, int n, float *verts, uint8_t *type,
                                  float4 *prims, Material *mats, cudaStream_t s);
 cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_count,
                               cudaStream_t s);
+// Segmented build: one LBVH per segment (scene) of the concatenated shape
+// arrays, all in one pass of each kernel.  btn holds the segments' internal
+// nodes back to back (segment s from seg_off[s] - s), btl their leaves (from
+// seg_off[s]), block_bounds / arrivals their per-level blocks (from bb_off[s]).
+// Every segment has at least two shapes.
+constexpr int kMaxSegments = 256;
+struct SegState { uint32_t cmin[3], cmax[3]; };
+struct SegBuild {
+    const int32_t *seg_off;     // n_segs + 1 shape offsets
+    const int32_t *tile_off;    // n_segs + 1 offsets of the segments' emission tiles
+    const int32_t *bb_off;      // n_segs + 1 offsets into block_bounds / arrivals
+    SegState *seg_state;        // n_segs
+    int32_t n_segs;
+    int32_t n_tiles;            // tile_off[n_segs]
+    int64_t n_blocks;           // bb_off[n_segs]
+};
+size_t seg_block_bound_count(int n);   // block_bound_count of one segment
+int emission_tiles(int n);             // emission tiles of one segment
+cudaError_t launch_lbvh_build_seg(const LbvhBuffers &b, int n_total, const SegBuild &sb,
+                                  int sm_count, cudaStream_t s);
 cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int *counters,
                            float *cost, int sweeps, cudaStream_t s);
+// node_base / shape_base: added to the child references and shape ids
+// written (a segment's place in the shared arrays of a batch; 0 otherwise)
 cudaError_t launch_abi_to_trace(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, int n,
                                 const float4 *prims0, float4 *nodes, float4 *prims,
-                                int32_t *prim_id, cudaStream_t s);
+                                int32_t *prim_id, cudaStream_t s, int node_base = 0,
+                                int shape_base = 0);
 cudaError_t launch_collapse4(const float4 *nodes2, int n_int, float4 *nodes4, cudaStream_t s);
 cudaError_t launch_gather_prims(const int32_t *order, int count, const float4 *prims0,
                                 float4 *prims, cudaStream_t s);
@@ -53,6 +79,22 @@ cudaError_t launch_export_shapes(ptgpu_shape *shapes, const float *verts, const 
                                  const uint32_t *keys, int n, cudaStream_t s);
 
 // trace.cu
+// One scene of a batched render.  Node, primitive, material and light
+// indices are global: the scenes' arrays are concatenated.
+struct BatchScene {
+    ptgpu_camera cam;
+    int32_t width, height, passes, max_depth;
+    int32_t start_sample;
+    int32_t root;               // global node index of the scene's root (>= 2 shapes)
+    int32_t n_shapes;
+    int32_t skip;               // global id of the scene's last shape
+    int32_t shape0;             // global id of the scene's first shape
+    int32_t light_first, n_lights;
+    int32_t pad;
+    int64_t pix_off;            // first pixel in colors/pixels; seeds at 2 * pix_off
+    float root_box[6];
+};
+
 struct RenderArgs {
     TraceView tv;
     const Material *mats;
@@ -71,8 +113,27 @@ struct RenderArgs {
     unsigned long long *stats;  // optional traversal counters (6 words)
     unsigned int *pixel_counter;// next pixel to hand out (zeroed per launch)
     int32_t max_ctas;           // grid cap (resident CTAs); 0 = one lane per pixel
+    int32_t refill;             // 32nds of a warp's live lanes that wait before it
+                                // shades (0: the default)
+    // batched render (scenes != null): the scene records in hand-out order,
+    // their first pixel in that order (n_scenes + 1 entries); the single-scene
+    // fields above (camera, size, passes, lights, depth, root) are unused
+    const BatchScene *scenes;
+    const int64_t *pix_start;
+    int32_t n_scenes;
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
+// A batched render (binary nodes; stack 32 or 64 entries) on `grid` resident
+// CTAs from render_batch_grid; the launch only enqueues stream work (the
+// pixel counter's reset and the kernel), so it can be captured in a graph.
+int render_batch_grid(int block, int stack, int max_ctas);
+cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int grid, cudaStream_t s);
+// batch.cu: each segment's root bound into its scene record; the deepest
+// leaf of every segment's tree (internal nodes on its path) into *depth
+cudaError_t launch_fill_roots(BatchScene *recs, int n, const ptgpu_bvh_node *btn, cudaStream_t s);
+cudaError_t launch_tree_depth(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl,
+                              const int32_t *seg_off, int n_segs, int n_total, int *depth,
+                              cudaStream_t s);
 
 // wavefront.cu: path state for `paths` slots (struct of arrays, carved from
 // one allocation of wf_carve_bytes) and the queues between the kernels
@@ -95,5 +156,10 @@ void wf_carve(WfArgs &a, void *base, int paths, int n_lights);
 cudaError_t launch_wavefront(WfArgs a, int iterations, int grid, cudaStream_t s);
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
                                  uint32_t *id, int32_t *hit, cudaStream_t s);
+
+// host helpers shared by the single-scene API and the batch (api.cpp)
+int record_error(int code, const std::string &msg);
+void make_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
+                 std::vector<LightRec> &lights);
 
 }  // namespace ptgpu

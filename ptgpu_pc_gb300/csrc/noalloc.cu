@@ -27,9 +27,6 @@
 
 namespace ptgpu {
 
-// api.cpp: records the message ptgpu_last_error() returns on this thread
-int record_error(int code, const std::string &msg);
-
 namespace {
 
 // 24.3 MiB are needed at kNoAllocMaxShapes; the rest is slack

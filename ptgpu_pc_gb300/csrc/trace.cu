@@ -70,28 +70,62 @@ enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 #ifndef PTGPU_RENDER_STEPS
 #define PTGPU_RENDER_STEPS 1
 #endif
-template <bool WIDE, bool COUNT>
+// The tracer proper.  BATCH: the lanes' pixels come from many scenes (scene
+// records in a.scenes, hand-out offsets in a.pix_start); otherwise from the
+// one scene of the single-scene fields.  STACK: traversal stack entries.
+constexpr int kMaxBatchScenes = 256;
+
+template <bool WIDE, bool COUNT, bool BATCH, int STACK>
 __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const RenderArgs a, unsigned int *pixel_counter) {
-    const int npx = a.width * a.height;
+    __shared__ int64_t s_start[BATCH ? kMaxBatchScenes + 1 : 1];
+    int64_t npx;
+    if (BATCH) {
+        for (int i = threadIdx.x; i <= a.n_scenes; i += blockDim.x) s_start[i] = a.pix_start[i];
+        __syncthreads();
+        npx = s_start[a.n_scenes];
+    } else {
+        npx = (int64_t)a.width * a.height;
+    }
     const int lane = threadIdx.x & 31;
-    const float inv_w = 1.f / (float)a.width, inv_h = 1.f / (float)a.height;
+    const int refill = a.refill > 0 ? a.refill : PTGPU_RENDER_REFILL;
     int state = ST_NEED;
     int gid = 0, passes_done = 0, depth = 0, li = 0, specular = 1;
+    int sc = 0;          // BATCH: the lane's scene (hand-out order)
     uint32_t s0 = 0, s1 = 0;
     f3 col = mk3(0.f, 0.f, 0.f), rad = col, tp = col, hp = col, nl = col;
     f3 ld = col, pend = col;
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
-    q.any = 0; q.hit = 0;
-    int stack[kStackSize];
+    q.any = 0; q.hit = 0; q.skip = -1;
+    int stack[STACK];
     bool trav = false;   // a query in flight
     bool fin = false;    // an answered query not yet consumed
     Counts cnt[3] = {{0, 0}, {0, 0}, {0, 0}};
 
+    // per-scene values: from the lane's scene record, or the single scene's
+    auto S = [&]() -> const BatchScene & { return a.scenes[sc]; };
+    auto width = [&]() { return BATCH ? __ldg(&S().width) : a.width; };
+    auto height = [&]() { return BATCH ? __ldg(&S().height) : a.height; };
+    auto pix_off = [&]() -> int64_t { return BATCH ? __ldg(&S().pix_off) : 0; };
+    auto max_depth = [&]() { return BATCH ? __ldg(&S().max_depth) : a.max_depth; };
+    auto n_lights = [&]() { return BATCH ? __ldg(&S().n_lights) : a.n_lights; };
+    auto start_sample = [&]() { return BATCH ? __ldg(&S().start_sample) : a.start_sample; };
+    auto passes = [&]() { return BATCH ? __ldg(&S().passes) : a.passes; };
+
     // starts a query; an immediately answered one is consumed like any other
     auto start = [&](f3 o, f3 d, bool any, float maxt) {
         Counts *c = cnt + (any ? 1 : 0);
-        if (trav_begin<COUNT>(a.tv, q, o, d, any, maxt, c)) fin = true;
+        TraceRoot root;
+        if (BATCH) {
+            root.first = __ldg(&S().root);
+            root.count = 0;
+            root.n_shapes = __ldg(&S().n_shapes);
+            root.skip = __ldg(&S().skip);
+            root.box = S().root_box;
+        } else {
+            root = view_root(a.tv);
+        }
+        if (trav_begin<COUNT>(a.tv, root, q, o, d, any, maxt, c)) fin = true;
         else trav = true;
     };
 
@@ -105,15 +139,27 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
             if (lane == leader) base = atomicAdd(pixel_counter, (unsigned)__popc(nm));
             base = __shfl_sync(0xffffffffu, base, leader);
             if (need) {
-                gid = (int)(base + __popc(nm & ((1u << lane) - 1u)));
-                if (gid >= npx) {
+                const int64_t g = (int64_t)base + __popc(nm & ((1u << lane) - 1u));
+                if (g >= npx) {
                     state = ST_DONE;
                 } else {
-                    const uint2 sd = reinterpret_cast<const uint2 *>(a.seeds)[gid];
+                    if (BATCH) {   // the scene whose hand-out range holds g
+                        int lo = 0, hi = a.n_scenes - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (s_start[mid] <= g) lo = mid; else hi = mid - 1;
+                        }
+                        sc = lo;
+                        gid = (int)(g - s_start[lo]);
+                    } else {
+                        gid = (int)g;
+                    }
+                    const uint2 sd = reinterpret_cast<const uint2 *>(a.seeds)[pix_off() + gid];
                     s0 = sd.x; s1 = sd.y;
-                    if (a.start_sample > 0) {
-                        const int x = gid % a.width, y = gid / a.width;
-                        const ptgpu_vec c = a.colors[(a.height - y - 1) * a.width + x];
+                    if (start_sample() > 0) {
+                        const int w = width(), h = height();
+                        const int x = gid % w, y = gid / w;
+                        const ptgpu_vec c = a.colors[pix_off() + (int64_t)(h - y - 1) * w + x];
                         col = mk3(c.x, c.y, c.z);
                     }
                     passes_done = 0;
@@ -127,8 +173,10 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
         if (!trav && !fin) {
             if (state == ST_GEN) {
                 // GenerateCameraRay (rendering_kernel.cl:1042-1070)
-                const int x = gid % a.width, y = gid / a.width;
-                const ptgpu_camera &cam = a.cam;
+                const int w = width(), h = height();
+                const float inv_w = 1.f / (float)w, inv_h = 1.f / (float)h;
+                const int x = gid % w, y = gid / w;
+                const ptgpu_camera &cam = BATCH ? S().cam : a.cam;
                 const float r1 = get_random(s0, s1) - .5f;
                 const float r2 = get_random(s0, s1) - .5f;
                 const float kcx = ((float)x + r1) * inv_w - .5f;
@@ -148,8 +196,10 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                 // SampleLights (rendering_kernel.cl:397-493): the next light
                 // that needs a visibility test
                 bool has_q = false;
-                while (li < a.n_lights) {
-                    const LightRec L = a.lights[li];
+                const int nlights = n_lights();
+                const LightRec *lights = BATCH ? a.lights + __ldg(&S().light_first) : a.lights;
+                while (li < nlights) {
+                    const LightRec L = lights[li];
                     float u1, u2;
                     if (a.rtl) { u2 = get_random(s0, s1); u1 = get_random(s0, s1); }
                     else       { u1 = get_random(s0, s1); u2 = get_random(s0, s1); }
@@ -207,7 +257,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                     f3 nd = add3(u, v);
                     w = smul3(sqrtf(1.f - r2), w);
                     nd = add3(nd, w);
-                    if (++depth > a.max_depth) {
+                    if (++depth > max_depth()) {
                         state = -1;   // pass finished
                     } else {
                         state = ST_EXT;
@@ -223,13 +273,13 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
             const unsigned busy = __ballot_sync(0xffffffffu, trav);
             if (!busy) break;
             const unsigned live = __ballot_sync(0xffffffffu, state != ST_DONE);
-            if (__popc(live & ~busy) * 32 >= PTGPU_RENDER_REFILL * __popc(live)) break;
-            if (trav && trav_step<WIDE, COUNT>(a.tv, q, stack, cnt + q.any)) {
+            if (__popc(live & ~busy) * 32 >= refill * __popc(live)) break;
+            if (trav && trav_step<WIDE, COUNT, STACK>(a.tv, q, stack, cnt + q.any)) {
                 trav = false;
                 fin = true;
             }
 #if PTGPU_RENDER_STEPS > 1
-            if (trav && trav_step<WIDE, COUNT>(a.tv, q, stack, cnt + q.any)) {
+            if (trav && trav_step<WIDE, COUNT, STACK>(a.tv, q, stack, cnt + q.any)) {
                 trav = false;
                 fin = true;
             }
@@ -249,11 +299,12 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                 const f3 d = q.d;
                 hp = add3(q.o, smul3(q.tb, d));
                 const int prim = q.prim;
-                const int id = prim >= 0 ? __ldg(&a.tv.prim_id[prim]) : 0;
+                const int shape0 = BATCH ? __ldg(&S().shape0) : 0;
+                const int id = prim >= 0 ? __ldg(&a.tv.prim_id[prim]) : shape0;
                 const Material m = a.mats[id];
                 const int type = __float_as_int(m.e_type.w);
                 const float4 *pp = prim >= 0 ? a.tv.prims : a.prims0;
-                const int k = prim >= 0 ? prim : 0;
+                const int k = prim >= 0 ? prim : shape0;
                 const float4 g0 = __ldg(&pp[3 * k + 0]);
                 f3 normal;
                 if (type == PTGPU_SPHERE) {
@@ -322,7 +373,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                             }
                         }
                     }
-                    if (++depth > a.max_depth) {
+                    if (++depth > max_depth()) {
                         state = -1;
                     } else {
                         if (COUNT) cnt[2].p++;
@@ -334,7 +385,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
 
         // ---- a finished pass: running mean, next pass or next pixel
         if (state == -1) {
-            const int cs = a.start_sample + passes_done;
+            const int cs = start_sample() + passes_done;
             if (cs == 0) {
                 col = rad;
             } else {
@@ -344,16 +395,18 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                 col.y = (col.y * k1 + rad.y) * k2;
                 col.z = (col.z * k1 + rad.z) * k2;
             }
-            if (++passes_done < a.passes) {
+            if (++passes_done < passes()) {
                 state = ST_GEN;
             } else {
-                const int x = gid % a.width, y = gid / a.width;
+                const int w = width(), h = height();
+                const int x = gid % w, y = gid / w;
+                const int64_t po = pix_off();
                 ptgpu_vec out;
                 out.x = col.x; out.y = col.y; out.z = col.z;
-                a.colors[(a.height - y - 1) * a.width + x] = out;
-                a.pixels[gid] = to_int(col.x) | (to_int(col.y) << 8) | (to_int(col.z) << 16) |
-                                0xff000000u;
-                reinterpret_cast<uint2 *>(a.seeds)[gid] = make_uint2(s0, s1);
+                a.colors[po + (int64_t)(h - y - 1) * w + x] = out;
+                a.pixels[po + gid] = to_int(col.x) | (to_int(col.y) << 8) | (to_int(col.z) << 16) |
+                                     0xff000000u;
+                reinterpret_cast<uint2 *>(a.seeds)[po + gid] = make_uint2(s0, s1);
                 state = ST_NEED;
             }
         }
@@ -368,6 +421,16 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     }
 }
 
+static int resident_grid(const void *kernel, int block, int max_ctas) {
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    int resident = per_sm * sms;
+    if (max_ctas > 0 && resident > max_ctas) resident = max_ctas;
+    return resident;
+}
+
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {
     const int n = a.width * a.height;
     if (n <= 0 || a.passes <= 0) return cudaSuccess;
@@ -375,26 +438,48 @@ cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {
     if (!a.pixel_counter) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(a.pixel_counter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    // lanes pull pixels until none remain; max_ctas caps the grid at what is resident
+    // lanes pull pixels until none remain; the grid is capped at what is resident
     const bool wide = a.tv.nodes4 != nullptr;
     int grid = (n + block - 1) / block;
-    int per_sm = 0, dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (wide) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render<true, false>, block, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render<false, false>, block, 0);
-    int resident = per_sm * sms;
-    if (a.max_ctas > 0 && resident > a.max_ctas) resident = a.max_ctas;
+    int resident = wide ? resident_grid((const void *)k_render<true, false, false, kStackSize>, block, a.max_ctas)
+                        : resident_grid((const void *)k_render<false, false, false, kStackSize>, block, a.max_ctas);
 #ifdef PTGPU_RENDER_GRID
     if (resident > PTGPU_RENDER_GRID) resident = PTGPU_RENDER_GRID;
 #endif
     if (resident > 0 && grid > resident) grid = resident;
     if (a.stats) {
-        if (wide) k_render<true, true><<<grid, block, 0, s>>>(a, a.pixel_counter);
-        else k_render<false, true><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        if (wide) k_render<true, true, false, kStackSize><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else k_render<false, true, false, kStackSize><<<grid, block, 0, s>>>(a, a.pixel_counter);
     } else {
-        if (wide) k_render<true, false><<<grid, block, 0, s>>>(a, a.pixel_counter);
-        else k_render<false, false><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        if (wide) k_render<true, false, false, kStackSize><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else k_render<false, false, false, kStackSize><<<grid, block, 0, s>>>(a, a.pixel_counter);
+    }
+    return cudaGetLastError();
+}
+
+// A batched render over a.n_scenes scene records (binary nodes only).  The
+// pixel counter is cleared on the stream first, so the pair can be captured
+// into a graph and replayed.
+int render_batch_grid(int block, int stack, int max_ctas) {
+    const void *k = stack > 32 ? (const void *)k_render<false, false, true, 64>
+                               : (const void *)k_render<false, false, true, 32>;
+    return resident_grid(k, block > 0 ? block : 128, max_ctas);
+}
+
+cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int grid, cudaStream_t s) {
+    if (!a.scenes || !a.pix_start || a.n_scenes <= 0 || a.n_scenes > kMaxBatchScenes)
+        return cudaErrorInvalidValue;
+    if (block <= 0) block = 128;
+    if (!a.pixel_counter || grid <= 0) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(a.pixel_counter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    const bool big = stack > 32;
+    if (a.stats) {
+        if (big) k_render<false, true, true, 64><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else k_render<false, true, true, 32><<<grid, block, 0, s>>>(a, a.pixel_counter);
+    } else {
+        if (big) k_render<false, false, true, 64><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else k_render<false, false, true, 32><<<grid, block, 0, s>>>(a, a.pixel_counter);
     }
     return cudaGetLastError();
 }

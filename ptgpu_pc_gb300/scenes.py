@@ -11,6 +11,7 @@ the same arrays feed the GPU library, the oracle and the reference's own code.
   random_rays(n)         seeded rays, origins in [-0.5,1.5]^3, uniform dirs
   batch_scenes()         64 mixed scenes (triangle counts log-uniform)
 """
+import functools
 import math
 
 import numpy as np
@@ -75,7 +76,10 @@ def _subdivide(v, f):
     """One loop of 1-to-4 subdivision with shared edge midpoints."""
     edges = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]], axis=0)
     key = np.sort(edges, axis=1)
-    uniq, inv = np.unique(key, axis=0, return_inverse=True)
+    # unique edges in (lo, hi) order, through one int64 code per edge
+    code = key[:, 0] * np.int64(len(v)) + key[:, 1]
+    ucode, inv = np.unique(code, return_inverse=True)
+    uniq = np.stack([ucode // len(v), ucode % len(v)], axis=1)
     mid = v[uniq[:, 0]] + v[uniq[:, 1]]
     mid /= np.linalg.norm(mid, axis=1, keepdims=True)
     base = len(v)
@@ -87,11 +91,19 @@ def _subdivide(v, f):
     return np.concatenate([v, mid], axis=0), nf
 
 
-def icosphere(level):
+@functools.lru_cache(maxsize=None)
+def _icosphere_cached(level):
     v, f = _icosahedron()
     for _ in range(level):
         v, f = _subdivide(v, f)
+    v.flags.writeable = False
+    f.flags.writeable = False
     return v, f
+
+
+def icosphere(level):
+    """Unit icosphere after `level` subdivisions (cached, read-only arrays)."""
+    return _icosphere_cached(level)
 
 
 def value_noise3(p, seed, freq):
@@ -155,8 +167,16 @@ def area_light(center=(50.0, 81.5, 80.0), half=10.0, emission=12.0):
 
 
 def displaced_icosphere(level=6, radius=20.0, center=(50.0, 25.0, 80.0), amp=0.05,
-                        freq=4.0, seed=2, albedo=0.75):
+                        freq=4.0, seed=2, albedo=0.75, faces=None):
+    """The icosphere radially displaced by value noise; `faces` keeps a subset
+    of its faces (the displacement of a vertex does not depend on which faces
+    are kept)."""
     v, f = icosphere(level)
+    if faces is not None:
+        f = f[faces]
+        used, f = np.unique(f, return_inverse=True)
+        f = f.reshape(-1, 3)
+        v = v[used]
     n = value_noise3(v, seed, freq)
     r = radius * (1.0 + amp * n)
     pts = v * r[:, None] + np.asarray(center)
@@ -169,11 +189,12 @@ def icosphere_scene(level=6, seed=2, n_tris=None):
     wall triangles and the 2 light triangles, in that order (the light last,
     where IntersectP does not test it).  n_tris subsamples the icosphere to an
     exact triangle count."""
-    ico = displaced_icosphere(level=level, seed=seed)
-    if n_tris is not None and n_tris < len(ico):
+    n_faces = 20 * 4 ** level
+    keep = None
+    if n_tris is not None and n_tris < n_faces:
         rng = np.random.default_rng(seed + 1000)
-        keep = np.sort(rng.choice(len(ico), n_tris, replace=False))
-        ico = ico[keep]
+        keep = np.sort(rng.choice(n_faces, n_tris, replace=False))
+    ico = displaced_icosphere(level=level, seed=seed, faces=keep)
     shapes = abi.concat_shapes(ico, box_walls(), area_light())
     cam = camera([50.0, 45.0, 168.0], pitch=0.2, yaw=0.0, target=[50.0, 25.0, 80.0])
     return shapes, 2, cam
