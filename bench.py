@@ -15,6 +15,9 @@ Extra keys on the JSON line:
   lbvh         LBVH build of 4,194,304 random triangles: Mtris/s and its HBM
                roofline at 252 algorithmic bytes per triangle
   closest_hit  2^24 random rays against the 4M-triangle BVH: Mrays/s
+  batched      64 mixed scenes (1k-2M triangles, 128^2-1024^2, 1-64 passes):
+               one batch (segmented build, one graph-replayed launch) against
+               the same scenes rendered one by one through contexts
   cpu_baseline the oracle port (C, OpenMP, all host threads) on a bounded
                sample of the same frame
 --impl reference times that CPU path alone (rank 0) on the same workload.
@@ -259,6 +262,72 @@ def bench_closest(ctx, torch, scenes, warmup, steps):
             "value": RAYS_N / m / 1e3, "unit": "Mrays/s", "ms": m, "hit_fraction": hits / RAYS_N}
 
 
+def bench_batched(pt, abi, scenes, torch, frames=2):
+    """The mixed-scene workload: 64 displaced-icosphere scenes drawn from
+    master seed 7 (1k-2M triangles log-uniform, 128^2..1024^2, 1..64 passes),
+    max depth 6.  Batched: one Batch (segmented build, tuned, graph-replayed
+    render).  Plain: the same scenes one after another through single-scene
+    contexts.  Both render the same samples from the same seeds."""
+    specs = scenes.batch_specs()
+    data = [scenes.scene_from_spec(sp) for sp in specs]
+    seeds = [pt.make_seeds(1000 + i, 2 * sp["res"] * sp["res"]) for i, sp in enumerate(specs)]
+    samples = float(sum(sp["res"] * sp["res"] * sp["spp"] for sp in specs))
+    shapes_total = int(sum(len(d[0]) for d in data))
+    # batched
+    t0 = time.perf_counter()
+    b = pt.Batch()
+    for (sh, lc, cam), sp, sd in zip(data, specs, seeds):
+        b.add(sh, lc, cam, sp["res"], sp["res"], sp["spp"], sd)
+    b.build(BUILD_FLAGS)
+    build_wall = time.perf_counter() - t0
+    build_ms = b.info()["build_ms"]
+    b.tune()
+    b.render()                                  # graph capture + warm-up
+    ms = []
+    for _ in range(frames):
+        b.reset()
+        t1 = time.perf_counter()
+        b.render()
+        ms.append((b.info()["render_ms"], time.perf_counter() - t1))
+    info = b.info()
+    b.close()
+    dev_ms = float(np.mean([m[0] for m in ms]))
+    frame_wall = float(np.mean([m[1] for m in ms]))
+    # plain: one context per scene, in turn
+    plain_dev_ms, plain_wall = 0.0, 0.0
+    for (sh, lc, cam), sp, sd in zip(data, specs, seeds):
+        t1 = time.perf_counter()
+        ctx = pt.Context(sp["res"], sp["res"], accel=abi.ACCEL_BVH)
+        ctx.set_shapes(sh, lc)
+        ctx.build(abi.ACCEL_BVH, BUILD_FLAGS)
+        ctx.set_camera(cam)
+        ctx.set_seeds(sd)
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.render_async(sp["spp"])
+        e1.record(stream)
+        e1.synchronize()
+        ctx.get_pixels()
+        plain_dev_ms += e0.elapsed_time(e1)
+        plain_wall += time.perf_counter() - t1
+        ctx.close()
+    return {"metric": "Msamples/s", "unit": "Msamples/s",
+            "workload": "64 scenes, master seed 7: %d shapes, %.1f M samples per frame, depth 6"
+                        % (shapes_total, samples / 1e6),
+            "value": samples / dev_ms / 1e3, "plain_value": samples / plain_dev_ms / 1e3,
+            "speedup_vs_plain": plain_dev_ms / dev_ms,
+            "e2e": {"value": samples / (build_wall + frame_wall) / 1e6,
+                    "plain_value": samples / plain_wall / 1e6,
+                    "per_step": "batched: add + segmented build + render; plain: per scene context, "
+                                "upload, build, render, pixels"},
+            "render_ms": dev_ms, "plain_render_ms": plain_dev_ms, "build_ms": build_ms,
+            "build_wall_s": build_wall, "frames": frames,
+            "tuned": {"block": info["block"], "refill": info["refill"], "stack": info["stack"],
+                      "tree_depth": info["tree_depth"]}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -268,6 +337,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-extras", action="store_true", help="skip lbvh/closest-hit/cpu legs")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched leg")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -388,6 +458,8 @@ def main():
         line["lbvh"] = lb
         line["closest_hit"] = bench_closest(lctx, torch, scenes, 1, 3)
         lctx.close()
+        if not args.no_batched:
+            line["batched"] = bench_batched(pt, abi, scenes, torch)
         if rank == 0:
             v, cores, desc = CpuReference(shapes, lc, cam, target_s=args.ref_seconds).sample()
             line["cpu_baseline"] = {"value": v, "unit": "Msamples/s", "cores": cores,

@@ -245,7 +245,7 @@ int  ptgpu_batch_add(ptgpu_batch *b, const ptgpu_scene *scene, int32_t *scene_id
 int  ptgpu_batch_build(ptgpu_batch *b, uint32_t flags);
 /* Times short one-pass renders of the batch over block sizes (64, 96, 128)
  * and refill thresholds (16, 20, 24 of 32 lanes), keeps the fastest, and
- * restores the seeds; the stack depth (32 or 64) follows the deepest tree.
+ * restores the seeds; the stack depth (32, 64 or 128) follows the deepest tree.
  * Resets the accumulation. */
 int  ptgpu_batch_tune(ptgpu_batch *b);
 /* One frame: each scene's `passes` passes, accumulated onto its running mean
@@ -256,6 +256,57 @@ int  ptgpu_batch_get_pixels(ptgpu_batch *b, int32_t scene, uint32_t *pixels);   
 int  ptgpu_batch_get_colors(ptgpu_batch *b, int32_t scene, ptgpu_vec *colors);  /* W*H, row-flipped */
 int  ptgpu_batch_get_bvh(ptgpu_batch *b, int32_t scene, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl);
 int  ptgpu_batch_info_get(ptgpu_batch *b, ptgpu_batch_info *info);
+
+/* ---- serving --------------------------------------------------------------- */
+/* No counterpart in the reference.  A server owns a worker thread that runs
+ * render requests with continuous batching: requests wait in arrival order,
+ * are admitted while their scene and their accumulation buffers fit the HBM
+ * budget, and every step renders up to `quantum` more passes of every
+ * admitted request in one launch, so requests that arrive while others run
+ * join at the next step.  Built scenes stay resident between requests under
+ * LRU (keyed by scene id) and are rebuilt after eviction.  A request's pixels
+ * depend only on its scene, camera, size, passes and seed: they equal a
+ * single-scene context's draw_frame(spp) after set_seeds(ptgpu_make_seeds(
+ * seed, 2*W*H)), alone or in any mix.  Submit and wait are thread-safe.     */
+typedef struct ptgpu_server ptgpu_server;
+
+typedef struct {
+    int32_t scene;              /* id from ptgpu_server_add_scene                */
+    int32_t width, height;
+    int32_t spp;                /* passes to render                              */
+    int32_t max_depth;          /* 0 selects PTGPU_MAX_DEPTH                     */
+    int32_t pad;
+    uint64_t seed;              /* master seed of the request's seed streams     */
+    ptgpu_camera camera;        /* orig/pitch/yaw; UpdateCamera runs on submit   */
+} ptgpu_request;
+
+typedef struct {
+    double queued_ms;           /* submit -> admission                           */
+    double latency_ms;          /* submit -> result ready                        */
+    int32_t steps;              /* render steps the request took part in         */
+    int32_t built;              /* 1: its scene was built for it (cache miss)    */
+} ptgpu_request_stats;
+
+typedef struct {
+    int64_t budget_bytes, bytes_in_use;
+    int64_t requests_done, builds, evictions, steps;
+    int32_t resident_scenes, active_requests, pending_requests, quantum;
+    double samples_done;
+} ptgpu_server_info;
+
+int  ptgpu_server_create(int32_t device, int64_t budget_bytes, int32_t quantum, uint32_t flags,
+                         ptgpu_server **out);  /* flags: PTGPU_FLAG_ARGS_RTL; quantum 0 = 4 */
+int  ptgpu_server_destroy(ptgpu_server *s);    /* finishes admitted work first */
+/* Registers a scene (copied); built on its first request with build_flags. */
+int  ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t n,
+                            uint32_t light_cnt, uint32_t build_flags, int32_t *scene);
+int  ptgpu_server_submit(ptgpu_server *s, const ptgpu_request *r, int64_t *ticket);
+/* Blocks until the request is done, copies its W*H pixels and colours (either
+ * may be NULL) and its stats, and forgets the ticket.  PTGPU_E_RANGE: the
+ * request can never fit the budget. */
+int  ptgpu_server_wait(ptgpu_server *s, int64_t ticket, uint32_t *pixels, ptgpu_vec *colors,
+                       ptgpu_request_stats *stats);
+int  ptgpu_server_info_get(ptgpu_server *s, ptgpu_server_info *info);
 
 /* ---- BVH build without device allocation ----------------------------------- */
 /* No counterpart in the reference.  The LBVH build of ptgpu_build(ctx,
@@ -305,6 +356,10 @@ PTGPU_SA(sizeof(ptgpu_scene) == 120, "ptgpu_scene is 120 bytes");
 PTGPU_SA(offsetof(ptgpu_scene, camera) == 16, "ptgpu_scene.camera at 16");
 PTGPU_SA(offsetof(ptgpu_scene, seeds) == 112, "ptgpu_scene.seeds at 112");
 PTGPU_SA(sizeof(ptgpu_batch_info) == 40, "ptgpu_batch_info is 40 bytes");
+PTGPU_SA(sizeof(ptgpu_request) == 112, "ptgpu_request is 112 bytes");
+PTGPU_SA(offsetof(ptgpu_request, camera) == 32, "ptgpu_request.camera at 32");
+PTGPU_SA(sizeof(ptgpu_request_stats) == 24, "ptgpu_request_stats is 24 bytes");
+PTGPU_SA(sizeof(ptgpu_server_info) == 72, "ptgpu_server_info is 72 bytes");
 #undef PTGPU_SA
 
 #endif /* PTGPU_H */

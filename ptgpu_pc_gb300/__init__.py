@@ -29,6 +29,8 @@ EXPORTS = [
     "ptgpu_batch_create", "ptgpu_batch_destroy", "ptgpu_batch_add", "ptgpu_batch_build",
     "ptgpu_batch_tune", "ptgpu_batch_render", "ptgpu_batch_reset", "ptgpu_batch_get_pixels",
     "ptgpu_batch_get_colors", "ptgpu_batch_get_bvh", "ptgpu_batch_info_get",
+    "ptgpu_server_create", "ptgpu_server_destroy", "ptgpu_server_add_scene", "ptgpu_server_submit",
+    "ptgpu_server_wait", "ptgpu_server_info_get",
 ]
 
 _lib = None
@@ -79,6 +81,12 @@ def lib():
         L.ptgpu_batch_get_colors.argtypes = [vp, i32, vp]
         L.ptgpu_batch_get_bvh.argtypes = [vp, i32, vp, vp]
         L.ptgpu_batch_info_get.argtypes = [vp, vp]
+        L.ptgpu_server_create.argtypes = [i32, ctypes.c_int64, i32, u32, ctypes.POINTER(vp)]
+        L.ptgpu_server_destroy.argtypes = [vp]
+        L.ptgpu_server_add_scene.argtypes = [vp, vp, u32, u32, u32, ctypes.POINTER(i32)]
+        L.ptgpu_server_submit.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_int64)]
+        L.ptgpu_server_wait.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
+        L.ptgpu_server_info_get.argtypes = [vp, vp]
         L.ptgpu_get_bvh.argtypes = [vp, vp, vp]
         L.ptgpu_set_bvh.argtypes = [vp, vp, vp, u32]
         L.ptgpu_get_kdtree.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]
@@ -356,6 +364,67 @@ class Batch:
     def close(self):
         if self._h:
             lib().ptgpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Render serving with continuous batching (ptgpu_server_* in
+    include/ptgpu.h): scenes registered once, built on first use and kept
+    resident under LRU within an HBM budget; submit() and wait() may be
+    called from any thread."""
+
+    def __init__(self, device=0, budget_bytes=120 << 30, quantum=0, flags=0):
+        self._h = ctypes.c_void_p()
+        _check(lib().ptgpu_server_create(device, budget_bytes, quantum, flags, ctypes.byref(self._h)))
+        self._sizes = {}
+
+    def add_scene(self, shapes, light_cnt, build_flags=0):
+        shapes = abi.as_struct(shapes, abi.SHAPE)
+        sid = ctypes.c_int32()
+        _check(lib().ptgpu_server_add_scene(self._h, shapes.ctypes.data, len(shapes), light_cnt,
+                                            build_flags, ctypes.byref(sid)))
+        return sid.value
+
+    def submit(self, scene, camera, width, height, spp, seed, max_depth=0):
+        r = np.zeros(1, abi.REQUEST)
+        r["scene"], r["width"], r["height"], r["spp"] = scene, width, height, spp
+        r["max_depth"], r["seed"] = max_depth, seed
+        r["camera"] = np.array(camera, abi.CAMERA)
+        t = ctypes.c_int64()
+        _check(lib().ptgpu_server_submit(self._h, r.ctypes.data, ctypes.byref(t)))
+        self._sizes[t.value] = (width, height)
+        return t.value
+
+    def wait(self, ticket, want_pixels=True, want_colors=True):
+        """Blocks until the request is done: (pixels, colours, stats)."""
+        w, h = self._sizes.pop(ticket)
+        px = np.zeros(w * h, np.uint32) if want_pixels else None
+        col = np.zeros((w * h, 3), np.float32) if want_colors else None
+        st = np.zeros(1, abi.REQUEST_STATS)
+        _check(lib().ptgpu_server_wait(self._h, ticket, px.ctypes.data if px is not None else None,
+                                       col.ctypes.data if col is not None else None, st.ctypes.data))
+        return px, col, {k: st[k][0].item() for k in abi.REQUEST_STATS.names}
+
+    def info(self):
+        out = np.zeros(1, abi.SERVER_INFO)
+        _check(lib().ptgpu_server_info_get(self._h, out.ctypes.data))
+        return {k: out[k][0].item() for k in abi.SERVER_INFO.names}
+
+    def close(self):
+        if self._h:
+            lib().ptgpu_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __enter__(self):

@@ -73,6 +73,29 @@ BATCH_INFO = np.dtype({
     "itemsize": 40,
 })
 
+# ptgpu_request / ptgpu_request_stats / ptgpu_server_info (serving)
+REQUEST = np.dtype({
+    "names": ["scene", "width", "height", "spp", "max_depth", "pad", "seed", "camera"],
+    "formats": ["<i4"] * 6 + ["<u8", CAMERA],
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 32],
+    "itemsize": 112,
+})
+
+REQUEST_STATS = np.dtype({
+    "names": ["queued_ms", "latency_ms", "steps", "built"],
+    "formats": ["<f8", "<f8", "<i4", "<i4"],
+    "offsets": [0, 8, 16, 20],
+    "itemsize": 24,
+})
+
+SERVER_INFO = np.dtype({
+    "names": ["budget_bytes", "bytes_in_use", "requests_done", "builds", "evictions", "steps",
+              "resident_scenes", "active_requests", "pending_requests", "quantum", "samples_done"],
+    "formats": ["<i8"] * 6 + ["<i4"] * 4 + ["<f8"],
+    "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 60, 64],
+    "itemsize": 72,
+})
+
 # status codes (include/ptgpu.h)
 OK, E_INVAL, E_OOM, E_DEVICE, E_TIMEOUT, E_IO, E_RANGE, E_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 

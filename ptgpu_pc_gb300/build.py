@@ -13,7 +13,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libptgpu.so")
 
 CU_SOURCES = ["lbvh.cu", "trace.cu", "wavefront.cu", "noalloc.cu", "batch.cu"]
-CPP_SOURCES = ["api.cpp", "kdtree.cpp", "loader.cpp", "batch.cpp"]
+CPP_SOURCES = ["api.cpp", "kdtree.cpp", "loader.cpp", "batch.cpp", "server.cpp"]
 HEADERS = ["device.cuh", "types.h", "lbvh.h", "lbvh_topo.cuh", "host.h", "devbuf.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # OpenCL C; IEEE division and square root are nvcc's defaults.
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-warn-spills"]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-pthread"]
 
 
 def _cuda_home():

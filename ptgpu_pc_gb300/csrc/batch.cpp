@@ -404,8 +404,7 @@ int ptgpu_batch_build(ptgpu_batch *b, uint32_t flags) {
     BK(cudaMemsetAsync(b->d_err.p, 0, 16, b->stream));
     BK(cudaStreamSynchronize(b->stream));
     b->tree_depth = depth;
-    // a binary traversal pushes at most two words per level
-    b->stack = (2 * depth + 2 <= 32) ? 32 : 64;
+    b->stack = render_stack_for_depth(depth);
     b->current.assign(S, 0);
     b->built = true;
     return PTGPU_OK;

@@ -123,9 +123,10 @@ struct RenderArgs {
     int32_t n_scenes;
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
-// A batched render (binary nodes; stack 32 or 64 entries) on `grid` resident
+// A batched render (binary nodes; stack 32, 64 or 128 entries) on `grid` resident
 // CTAs from render_batch_grid; the launch only enqueues stream work (the
 // pixel counter's reset and the kernel), so it can be captured in a graph.
+int render_stack_for_depth(int depth);   // 32, 64 or 128 entries for a tree depth
 int render_batch_grid(int block, int stack, int max_ctas);
 cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int grid, cudaStream_t s);
 // batch.cu: each segment's root bound into its scene record; the deepest

@@ -460,8 +460,14 @@ cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {
 // A batched render over a.n_scenes scene records (binary nodes only).  The
 // pixel counter is cleared on the stream first, so the pair can be captured
 // into a graph and replayed.
+int render_stack_for_depth(int depth) {
+    const int words = 2 * depth + 2;   // at most one push of <= 2 words per level
+    return words <= 32 ? 32 : (words <= 64 ? 64 : 128);
+}
+
 int render_batch_grid(int block, int stack, int max_ctas) {
-    const void *k = stack > 32 ? (const void *)k_render<false, false, true, 64>
+    const void *k = stack > 64 ? (const void *)k_render<false, false, true, 128>
+                  : stack > 32 ? (const void *)k_render<false, false, true, 64>
                                : (const void *)k_render<false, false, true, 32>;
     return resident_grid(k, block > 0 ? block : 128, max_ctas);
 }
@@ -473,12 +479,13 @@ cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int g
     if (!a.pixel_counter || grid <= 0) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(a.pixel_counter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    const bool big = stack > 32;
     if (a.stats) {
-        if (big) k_render<false, true, true, 64><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        if (stack > 64) k_render<false, true, true, 128><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else if (stack > 32) k_render<false, true, true, 64><<<grid, block, 0, s>>>(a, a.pixel_counter);
         else k_render<false, true, true, 32><<<grid, block, 0, s>>>(a, a.pixel_counter);
     } else {
-        if (big) k_render<false, false, true, 64><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        if (stack > 64) k_render<false, false, true, 128><<<grid, block, 0, s>>>(a, a.pixel_counter);
+        else if (stack > 32) k_render<false, false, true, 64><<<grid, block, 0, s>>>(a, a.pixel_counter);
         else k_render<false, false, true, 32><<<grid, block, 0, s>>>(a, a.pixel_counter);
     }
     return cudaGetLastError();
