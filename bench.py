@@ -18,6 +18,11 @@ Extra keys on the JSON line:
   batched      64 mixed scenes (1k-2M triangles, 128^2-1024^2, 1-64 passes):
                one batch (segmented build, one graph-replayed launch) against
                the same scenes rendered one by one through contexts
+  served       Poisson request streams over those scenes (10, 100, 1000 req/s,
+               70% of requests on an already requested scene): the server
+               (continuous batching, 120 GB budget, LRU scene cache) against
+               the plain path (first come first served, a context per
+               request); throughput and p50/p99 latency
   cpu_baseline the oracle port (C, OpenMP, all host threads) on a bounded
                sample of the same frame
 --impl reference times that CPU path alone (rank 0) on the same workload.
@@ -262,6 +267,86 @@ def bench_closest(ctx, torch, scenes, warmup, steps):
             "value": RAYS_N / m / 1e3, "unit": "Mrays/s", "ms": m, "hit_fraction": hits / RAYS_N}
 
 
+def served_requests(specs, n_req, rate, seed=5, hit=0.7):
+    """A seeded request stream over the 64 config scenes: Poisson arrivals at
+    `rate` per second; each request reuses an already requested scene with
+    probability `hit` (else the next new one) and draws its resolution and
+    passes from the config distribution."""
+    from ptgpu_pc_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    t, seen, nxt, out = 0.0, [], 0, []
+    for i in range(n_req):
+        t += rng.exponential(1.0 / rate)
+        if seen and (rng.random() < hit or nxt >= len(specs)):
+            sc = int(seen[rng.integers(len(seen))])
+        else:
+            sc = nxt
+            nxt += 1
+            seen.append(sc)
+        res = int(rng.choice(scenes.RESOLUTIONS))
+        spp = int(rng.choice(scenes.SPPS))
+        out.append(dict(t=t, scene=sc, res=res, spp=spp, seed=7000 + i))
+    return out
+
+
+def bench_served(pt, abi, data, specs, rates=(10, 100, 1000), n_req=48):
+    """Requests arriving at each rate, served with continuous batching (one
+    server, 120 GB budget, scenes resident under LRU) and, for comparison,
+    by the plain path: one request after another, each building its scene in
+    a fresh context.  Both produce the same pixels for a request (same seed
+    streams), so the image error is equal by construction."""
+    out = []
+    for rate in rates:
+        reqs = served_requests(specs, n_req, rate)
+        samples = float(sum(r["res"] * r["res"] * r["spp"] for r in reqs))
+        # served
+        srv = pt.Server(budget_bytes=120 << 30)
+        ids = {}
+        for r in reqs:
+            if r["scene"] not in ids:
+                sh, lc, _ = data[r["scene"]]
+                ids[r["scene"]] = srv.add_scene(sh, lc, BUILD_FLAGS)
+        tickets = []
+        t0 = time.perf_counter()
+        for r in reqs:
+            while time.perf_counter() - t0 < r["t"]:
+                time.sleep(min(0.002, max(0.0, r["t"] - (time.perf_counter() - t0))))
+            cam = data[r["scene"]][2]
+            tickets.append(srv.submit(ids[r["scene"]], cam, r["res"], r["res"], r["spp"], r["seed"]))
+        lat = []
+        for tk in tickets:
+            _, _, st = srv.wait(tk, want_pixels=False, want_colors=False)
+            lat.append(st["latency_ms"])
+        span = time.perf_counter() - t0
+        info = srv.info()
+        srv.close()
+        # plain: first come, first served, one context per request
+        plat = []
+        t0 = time.perf_counter()
+        for r in reqs:
+            now = time.perf_counter() - t0
+            if now < r["t"]:
+                time.sleep(r["t"] - now)
+            sh, lc, cam = data[r["scene"]]
+            ctx = pt.Context(r["res"], r["res"], accel=abi.ACCEL_BVH)
+            ctx.set_shapes(sh, lc)
+            ctx.build(abi.ACCEL_BVH, BUILD_FLAGS)
+            ctx.set_camera(cam)
+            ctx.set_seeds(pt.make_seeds(r["seed"], 2 * r["res"] * r["res"]))
+            ctx.draw_frame_view(r["spp"])
+            ctx.close()
+            plat.append((time.perf_counter() - t0 - r["t"]) * 1e3)
+        pspan = time.perf_counter() - t0
+        out.append({"rate_per_s": rate, "requests": n_req,
+                    "value": samples / span / 1e6, "plain_value": samples / pspan / 1e6,
+                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                    "plain_p50_ms": float(np.percentile(plat, 50)),
+                    "plain_p99_ms": float(np.percentile(plat, 99)),
+                    "builds": info["builds"], "steps": info["steps"],
+                    "scene_hits": 1.0 - info["builds"] / n_req})
+    return out
+
+
 def bench_batched(pt, abi, scenes, torch, frames=2):
     """The mixed-scene workload: 64 displaced-icosphere scenes drawn from
     master seed 7 (1k-2M triangles log-uniform, 128^2..1024^2, 1..64 passes),
@@ -313,7 +398,7 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
         plain_dev_ms += e0.elapsed_time(e1)
         plain_wall += time.perf_counter() - t1
         ctx.close()
-    return {"metric": "Msamples/s", "unit": "Msamples/s",
+    return data, specs, {"metric": "Msamples/s", "unit": "Msamples/s",
             "workload": "64 scenes, master seed 7: %d shapes, %.1f M samples per frame, depth 6"
                         % (shapes_total, samples / 1e6),
             "value": samples / dev_ms / 1e3, "plain_value": samples / plain_dev_ms / 1e3,
@@ -459,7 +544,8 @@ def main():
         line["closest_hit"] = bench_closest(lctx, torch, scenes, 1, 3)
         lctx.close()
         if not args.no_batched:
-            line["batched"] = bench_batched(pt, abi, scenes, torch)
+            data, specs, line["batched"] = bench_batched(pt, abi, scenes, torch)
+            line["served"] = bench_served(pt, abi, data, specs)
         if rank == 0:
             v, cores, desc = CpuReference(shapes, lc, cam, target_s=args.ref_seconds).sample()
             line["cpu_baseline"] = {"value": v, "unit": "Msamples/s", "cores": cores,
