@@ -676,7 +676,8 @@ int ptgpu_trace_closest_device(ptgpu_ctx *c, const ptgpu_ray *d_rays, uint32_t n
     if (!c || (n && (!d_rays || !d_t || !d_id || !d_hit))) return fail(PTGPU_E_INVAL, "null argument");
     if (c->accel_built < 0) return fail(PTGPU_E_STATE, "build an acceleration structure first");
     cudaSetDevice(c->device);
-    CK(launch_trace_closest(make_view(c), d_rays, (int)n, d_t, d_id, d_hit, c->stream));
+    CK(launch_trace_closest(make_view(c), d_rays, (int)n, d_t, d_id, d_hit, c->stream,
+                            c->d_pixctr.as<unsigned int>() + 1));
     return PTGPU_OK;
 }
 
@@ -692,7 +693,8 @@ int ptgpu_trace_closest(ptgpu_ctx *c, const ptgpu_ray *rays, uint32_t n, float *
     CK(c->d_hit.ensure((size_t)n * 4));
     CK(cudaMemcpyAsync(c->d_rays.p, rays, (size_t)n * sizeof(ptgpu_ray), cudaMemcpyHostToDevice, c->stream));
     CK(launch_trace_closest(make_view(c), c->d_rays.as<ptgpu_ray>(), (int)n, c->d_t.as<float>(),
-                            c->d_id.as<uint32_t>(), c->d_hit.as<int32_t>(), c->stream));
+                            c->d_id.as<uint32_t>(), c->d_hit.as<int32_t>(), c->stream,
+                            c->d_pixctr.as<unsigned int>() + 1));
     CK(cudaMemcpyAsync(t, c->d_t.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(id, c->d_id.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(hit, c->d_hit.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));

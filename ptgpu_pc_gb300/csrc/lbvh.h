@@ -155,8 +155,10 @@ constexpr int kWfMaxLights = 8;
 size_t wf_carve_bytes(int paths, int n_lights);
 void wf_carve(WfArgs &a, void *base, int paths, int n_lights);
 cudaError_t launch_wavefront(WfArgs a, int iterations, int grid, cudaStream_t s);
+// counter: a device word for the persistent kernel (null: one thread per ray)
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
-                                 uint32_t *id, int32_t *hit, cudaStream_t s);
+                                 uint32_t *id, int32_t *hit, cudaStream_t s,
+                                 unsigned int *counter = nullptr);
 
 // host helpers shared by the single-scene API and the batch (api.cpp)
 int record_error(int code, const std::string &msg);

@@ -491,11 +491,86 @@ cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int g
     return cudaGetLastError();
 }
 
+// Closest hits of a ray batch with persistent lanes: each lane takes the
+// next ray from a global counter (one atomicAdd per warp), and a warp steps
+// its rays' traversals until `refill`/32 of its live lanes are idle, then
+// writes their results and refills them together -- the render kernel's
+// schedule without the shading.  Each ray visits its nodes in the same order
+// as in trace_query.
+template <bool WIDE>
+__global__ void __launch_bounds__(128) k_trace_closest_p(TraceView tv,
+                                                          const ptgpu_ray *__restrict__ rays,
+                                                          int n, float *__restrict__ tout,
+                                                          uint32_t *__restrict__ idout,
+                                                          int32_t *__restrict__ hitout,
+                                                          unsigned int *counter, int refill) {
+    const int lane = threadIdx.x & 31;
+    const TraceRoot root = view_root(tv);
+    Trav q;
+    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0; q.skip = -1;
+    int stack[kStackSize];
+    int ray = -1;
+    bool trav = false, fin = false, done = false;
+    for (;;) {
+        const bool need = !trav && !fin && !done;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        if (nm) {
+            const int leader = __ffs(nm) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(nm));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const int64_t r = (int64_t)base + __popc(nm & ((1u << lane) - 1u));
+                if (r >= n) {
+                    done = true;
+                } else {
+                    ray = (int)r;
+                    const float *rp = reinterpret_cast<const float *>(rays + ray);
+                    const f3 o = mk3(rp[0], rp[1], rp[2]);
+                    const f3 d = mk3(rp[3], rp[4], rp[5]);
+                    if (trav_begin<false>(tv, root, q, o, d, false, 0.f, nullptr)) fin = true;
+                    else trav = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        for (;;) {
+            const unsigned busy = __ballot_sync(0xffffffffu, trav);
+            if (!busy) break;
+            const unsigned live = __ballot_sync(0xffffffffu, !done);
+            if (__popc(live & ~busy) * 32 >= refill * __popc(live)) break;
+            if (trav && trav_step<WIDE, false>(tv, q, stack, nullptr)) {
+                trav = false;
+                fin = true;
+            }
+        }
+        if (fin) {
+            fin = false;
+            tout[ray] = q.tb;
+            idout[ray] = (q.hit && q.prim >= 0) ? (uint32_t)__ldg(&tv.prim_id[q.prim]) : 0u;
+            hitout[ray] = q.hit;
+        }
+    }
+}
+
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
-                                 uint32_t *id, int32_t *hit, cudaStream_t s) {
+                                 uint32_t *id, int32_t *hit, cudaStream_t s, unsigned int *counter) {
     if (n <= 0) return cudaSuccess;
-    if (tv.nodes4) k_trace_closest<true><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
-    else k_trace_closest<false><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
+    if (!counter) {   // one thread per ray
+        if (tv.nodes4) k_trace_closest<true><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
+        else k_trace_closest<false><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    const void *k = tv.nodes4 ? (const void *)k_trace_closest_p<true> : (const void *)k_trace_closest_p<false>;
+    int grid = resident_grid(k, 128, 0);
+    const int need = (n + 127) / 128;
+    if (grid <= 0 || grid > need) grid = need;
+    if (tv.nodes4)
+        k_trace_closest_p<true><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, PTGPU_RENDER_REFILL);
+    else
+        k_trace_closest_p<false><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, PTGPU_RENDER_REFILL);
     return cudaGetLastError();
 }
 
