@@ -72,7 +72,7 @@ struct ptgpu_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float build_ms = 0.f, render_ms = 0.f;
     // device arrays
-    DevBuf d_shapes, d_verts, d_type, d_aabbs, d_prims0, d_mats, d_lights;
+    DevBuf d_shapes, d_verts, d_type, d_aabbs, d_lb, d_prims0, d_mats, d_lights;
     DevBuf d_btn, d_btl, d_keys, d_keys_alt, d_keys_tmp, d_vals_alt, d_vals_tmp, d_sorted;
     DevBuf d_status, d_state, d_block_bounds, d_arrivals, d_tcount, d_tcost;
     DevBuf d_seg_off, d_tile_off, d_bb_off, d_seg_state, d_depth;
@@ -164,7 +164,7 @@ int ptgpu_batch_destroy(ptgpu_batch *b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     b->drop_graph();
-    DevBuf *bufs[] = {&b->d_shapes, &b->d_verts, &b->d_type, &b->d_aabbs, &b->d_prims0, &b->d_mats,
+    DevBuf *bufs[] = {&b->d_shapes, &b->d_verts, &b->d_type, &b->d_aabbs, &b->d_lb, &b->d_prims0, &b->d_mats,
                       &b->d_lights, &b->d_btn, &b->d_btl, &b->d_keys, &b->d_keys_alt, &b->d_keys_tmp,
                       &b->d_vals_alt, &b->d_vals_tmp, &b->d_sorted, &b->d_status, &b->d_state,
                       &b->d_block_bounds, &b->d_arrivals, &b->d_tcount, &b->d_tcost, &b->d_seg_off,
@@ -259,6 +259,7 @@ int ptgpu_batch_build(ptgpu_batch *b, uint32_t flags) {
     BK(b->d_verts.ensure(N * 9 * sizeof(float)));
     BK(b->d_type.ensure(N));
     BK(b->d_aabbs.ensure(N * 2 * sizeof(float4)));
+    BK(b->d_lb.ensure(N * 2 * sizeof(float4)));
     BK(b->d_prims0.ensure(N * 3 * sizeof(float4)));
     BK(b->d_mats.ensure(N * sizeof(Material)));
     BK(b->d_lights.ensure(std::max<size_t>(1, lights.size()) * sizeof(LightRec)));
@@ -312,6 +313,7 @@ int ptgpu_batch_build(ptgpu_batch *b, uint32_t flags) {
     lb.verts = b->d_verts.as<float>();
     lb.type = b->d_type.as<uint8_t>();
     lb.aabbs = b->d_aabbs.as<float4>();
+    lb.leaf_bounds = b->d_lb.as<float4>();
     lb.keys = b->d_keys.as<uint32_t>();
     lb.keys_alt = b->d_keys_alt.as<uint32_t>();
     lb.keys_tmp = b->d_keys_tmp.as<uint32_t>();

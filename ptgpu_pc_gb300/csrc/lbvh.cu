@@ -9,12 +9,13 @@
 //                       stable bubble sort, CLBVH.cpp:31-47), 8-bit digits,
 //                       warp-level ranking through shared lane masks,
 //                       decoupled look-back with a bounded spin
-//   k_tiles             per 1024-leaf tile: leaf records + every internal node
-//                       inside the tile, bounds by an in-shared-memory
-//                       bottom-up reduction, then a climb over the tiles for
-//                       the nodes above them (kernelConstructRadixTree and
-//                       kernelConstructBVHTree, BVH.cl:141-258, with the
-//                       closed-form topology of lbvh_topo.cuh)
+//   k_leaves            leaf records, and the leaves' bounds in sorted order
+//   k_tiles             per 1024-leaf tile: every internal node inside the
+//                       tile, bounds by a warp-shuffle bottom-up reduction,
+//                       then a climb over the tiles for the nodes above them
+//                       (kernelConstructRadixTree and kernelConstructBVHTree,
+//                       BVH.cl:141-258, with the closed-form topology of
+//                       lbvh_topo.cuh)
 // The result is the reference's btn[N-1]/btl[N] arrays, resident on the
 // device.  k_abi_to_trace then derives the 64-byte traversal nodes.
 #include <cfloat>
@@ -604,14 +605,12 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
 // bound goes to a per-level array, and of the two tiles (then blocks) under
 // a parent the one that arrives second merges them and moves up.
 // ---------------------------------------------------------------------------
-#ifndef PTGPU_TILE_LOG
-#define PTGPU_TILE_LOG 10
-#endif
-constexpr int kTileLog = PTGPU_TILE_LOG;
+constexpr int kTileLog = 10;
 constexpr int kTileLeaves = 1 << kTileLog;
 constexpr int kTileThreads = kTileLeaves / 2;   // two leaves per thread
 constexpr int kRecWords = 15;
-constexpr size_t kTileSmem = (6 * kTileLeaves) * sizeof(float) + kTileLeaves * kRecWords * 4 + kTileLeaves;
+// staged records, the 16 warps' bounds, node flags
+constexpr size_t kTileSmem = kTileLeaves * kRecWords * 4 + 16 * 6 * sizeof(float) + kTileLeaves;
 
 __device__ __forceinline__ void write_node(ptgpu_bvh_node *dst, int mn, int mx, int nshape, int leaf,
                                            int nl, int nr, int np, const float b[6], uint32_t cost_bits,
@@ -658,93 +657,145 @@ __device__ __forceinline__ int level_offset(int level, int ntiles) {
     return off;
 }
 
-// One tile of one tree: `tile` counts the tree's tiles, `sorted` is the
-// tree's part of the sorted shape ids, whose values start at shape_base (the
-// leaves' nShape is the id minus shape_base); btn/btl/block_bounds/arrivals
-// are the tree's own arrays.
-__device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ aabbs,
-                                          const int32_t *__restrict__ sorted, int shape_base, int n,
+// Leaf records of every tree, and the leaves' bounds in sorted order for the
+// tile kernel: one thread per leaf gathers its shape's 32-byte bound; the
+// 60-byte records leave through shared memory as coalesced words.  With
+// n_segs > 0 the leaves belong to the segments of seg_off (record fields are
+// segment-local), otherwise to one tree of n_total leaves.
+constexpr int kLeafThreads = 256;
+__global__ void __launch_bounds__(kLeafThreads) k_leaves(const float4 *__restrict__ aabbs,
+                                                          const int32_t *__restrict__ sorted,
+                                                          int n_total, const int32_t *__restrict__ seg_off,
+                                                          int n_segs, ptgpu_bvh_node *__restrict__ btl,
+                                                          float4 *__restrict__ lb) {
+    __shared__ uint32_t rec[kLeafThreads * kRecWords];
+    __shared__ int32_t s_off[kMaxSegments + 1];
+    if (n_segs > 0) {
+        for (int i = threadIdx.x; i <= n_segs; i += kLeafThreads) s_off[i] = seg_off[i];
+        __syncthreads();
+    }
+    const int k0 = blockIdx.x * kLeafThreads;
+    const int k = k0 + threadIdx.x;
+    if (k < n_total) {
+        int off = 0, n = n_total;
+        if (n_segs > 0) {
+            const int g = (int)segment_of(s_off, n_segs, k);
+            off = s_off[g];
+            n = s_off[g + 1] - off;
+        }
+        // in bounds even after a failed sort
+        const int sh = min(max(__ldg(sorted + k) - off, 0), n - 1) + off;
+        const float4 q0 = __ldg(aabbs + 2 * (size_t)sh), q1 = __ldg(aabbs + 2 * (size_t)sh + 1);
+        lb[2 * (size_t)k] = q0;
+        lb[2 * (size_t)k + 1] = q1;
+        const float b[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+        const int parent = n >= 2 ? topo_parent_leaf(k - off, n) : -1;
+        stage_node(rec + threadIdx.x * kRecWords, -1, -1, sh - off, -1, -1, -1, parent, b, 0xffffffffu,
+                   0xffffffffu);
+    }
+    __syncthreads();
+    const int cnt = min(kLeafThreads, n_total - k0);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(btl + k0);
+    for (int w = threadIdx.x; w < cnt * kRecWords; w += kLeafThreads) dst[w] = rec[w];
+}
+
+// One tile of one tree: `tile` counts the tree's tiles, `lb` holds the tree's
+// leaf bounds in sorted order; btn/block_bounds/arrivals are the tree's own
+// arrays.  The tile's internal nodes are the blocks of 2^L leaves at levels
+// L = 1..10 (the index-prefix topology).  Thread t holds the leaves
+// [2t, 2t+1]; levels 2-6 merge a block with its right neighbour's bound, held
+// 2^(L-2) lanes up (shuffle); levels 7-10 run in warp 0 over the 16 warps'
+// bounds.  A block whose right half is empty creates no node and keeps its
+// bound.  Records are staged in shared memory (the active lanes of a level
+// are 2^(L-1) apart, so a staging store meets at most two lanes per bank)
+// and copied out as coalesced words.
+__device__ __forceinline__ void block_record(uint32_t *rec, unsigned char *own, int T0, int l0,
+                                             int level, int n, const float b[6]) {
+    const int lo = T0 + l0;
+    const int hi = min(T0 + l0 + (1 << level), n) - 1;
+    const BlockNode bn = block_node(lo, hi, level, n);
+    const int j = bn.idx - T0;
+    if (bn.idx >= 0 && bn.idx < n - 1 && j >= 0 && j < kTileLeaves) {   // internal, in the tile
+        stage_node(rec + j * kRecWords, lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
+        own[j] = 1;
+    }
+}
+
+__device__ __forceinline__ void shfl_down6(float *c, const float *b, int off) {
+#pragma unroll
+    for (int a = 0; a < 6; ++a) c[a] = __shfl_down_sync(0xffffffffu, b[a], off);
+}
+
+__device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ lb, int n,
                                           ptgpu_bvh_node *__restrict__ btn,
-                                          ptgpu_bvh_node *__restrict__ btl,
                                           float *__restrict__ block_bounds,
                                           uint32_t *__restrict__ arrivals, int ntiles,
                                           unsigned char *tsm) {
-    float *sb = reinterpret_cast<float *>(tsm);                          // [6][1024]
-    uint32_t *rec = reinterpret_cast<uint32_t *>(sb + 6 * kTileLeaves);  // [1024][15]
-    unsigned char *own = reinterpret_cast<unsigned char *>(rec + kTileLeaves * kRecWords);
+    static_assert(kTileLeaves == 1024 && kTileThreads == 512, "16 warps of 64 leaves");
+    uint32_t *rec = reinterpret_cast<uint32_t *>(tsm);                      // [1024][15]
+    float *wb = reinterpret_cast<float *>(rec + kTileLeaves * kRecWords);    // [16][6]
+    unsigned char *own = reinterpret_cast<unsigned char *>(wb + 16 * 6);     // [1024]
     const int T0 = tile * kTileLeaves;
     const int cnt = min(kTileLeaves, n - T0);
-    const int tid = threadIdx.x;
-    // ---- leaves: both of a thread's gathers are issued before either is used
-    {
-        int sh[2];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int k = tid + u * kTileThreads;
-            // in bounds even after a failed sort
-            sh[u] = k < cnt ? min(max(__ldg(sorted + T0 + k) - shape_base, 0), n - 1) + shape_base
-                            : shape_base;
-        }
-        float4 q[2][2];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            q[u][0] = __ldg(aabbs + 2 * (size_t)sh[u]);
-            q[u][1] = __ldg(aabbs + 2 * (size_t)sh[u] + 1);
-        }
-        float b[2][6];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            b[u][0] = q[u][0].x; b[u][1] = q[u][0].y; b[u][2] = q[u][0].z;
-            b[u][3] = q[u][0].w; b[u][4] = q[u][1].x; b[u][5] = q[u][1].y;
-        }
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int k = tid + u * kTileThreads;
-            if (k >= cnt) continue;
-            for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + k] = b[u][a];
-            const int parent = n >= 2 ? topo_parent_leaf(T0 + k, n) : -1;
-            stage_node(rec + k * kRecWords, -1, -1, sh[u] - shape_base, -1, -1, -1, parent, b[u], 0xffffffffu,
-                       0xffffffffu);
-            own[k] = 0;
-        }
-    }
-    __syncthreads();
-    {
-        uint32_t *dst = reinterpret_cast<uint32_t *>(btl + T0);
-        for (int w = tid; w < cnt * kRecWords; w += kTileThreads) dst[w] = rec[w];
-    }
-    __syncthreads();
-    // ---- internal nodes inside the tile
-    for (int level = 1; level <= kTileLog; ++level) {
-        const int half = 1 << (level - 1);
-        const int nblk = (cnt + (1 << level) - 1) >> level;
-        for (int bidx = tid; bidx < nblk; bidx += kTileThreads) {
-            const int l0 = bidx << level, r0 = l0 + half;
-            if (r0 >= cnt) continue;                       // right half empty: same set
-            float b[6], c[6];
-            for (int a = 0; a < 6; ++a) { b[a] = sb[a * kTileLeaves + l0]; c[a] = sb[a * kTileLeaves + r0]; }
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    own[2 * tid] = 0;
+    own[2 * tid + 1] = 0;
+    // ---- level 1: a thread's two leaves
+    const int l0 = 2 * tid;
+    float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, c[6];
+    bool have = l0 < cnt;
+    if (have) {
+        const float4 *p = lb + 2 * (size_t)(T0 + l0);
+        const float4 q0 = __ldg(p), q1 = __ldg(p + 1);
+        b[0] = q0.x; b[1] = q0.y; b[2] = q0.z; b[3] = q0.w; b[4] = q1.x; b[5] = q1.y;
+        if (l0 + 1 < cnt) {
+            const float4 r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+            c[0] = r0.x; c[1] = r0.y; c[2] = r0.z; c[3] = r0.w; c[4] = r1.x; c[5] = r1.y;
             merge6(b, c);
-            for (int a = 0; a < 6; ++a) sb[a * kTileLeaves + l0] = b[a];
-            const int lo = T0 + l0;
-            const int hi = min(T0 + l0 + (1 << level), n) - 1;
-            const BlockNode bn = block_node(lo, hi, level, n);
-            const int j = bn.idx - T0;
-            stage_node(rec + j * kRecWords, lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b,
-                       0u, 0u);
-            own[j] = 1;
         }
-        __syncthreads();
     }
+    __syncthreads();                                // own[] cleared
+    if (have && l0 + 1 < cnt) block_record(rec, own, T0, l0, 1, n, b);
+    // ---- levels 2-6 inside the warp
+#pragma unroll
+    for (int level = 2; level <= 6; ++level) {
+        const int off = 1 << (level - 2);           // lanes between a block's halves
+        shfl_down6(c, b, off);
+        const bool leader = (lane & ((off << 1) - 1)) == 0;
+        if (leader && have && l0 + (1 << (level - 1)) < cnt) {
+            merge6(b, c);
+            block_record(rec, own, T0, l0, level, n, b);
+        }
+    }
+    if (lane == 0 && have)
+        for (int a = 0; a < 6; ++a) wb[w * 6 + a] = b[a];
+    __syncthreads();
+    // ---- levels 7-10 over the 16 warps, in warp 0
+    if (w == 0) {
+        const int wl0 = 64 * lane;                  // lane j holds warp j's block
+        have = lane < 16 && wl0 < cnt;
+        if (have)
+            for (int a = 0; a < 6; ++a) b[a] = wb[lane * 6 + a];
+#pragma unroll
+        for (int level = 7; level <= 10; ++level) {
+            const int off = 1 << (level - 7);
+            shfl_down6(c, b, off);
+            const bool leader = (lane & ((off << 1) - 1)) == 0;
+            if (leader && have && wl0 + (1 << (level - 1)) < cnt) {
+                merge6(b, c);
+                block_record(rec, own, T0, wl0, level, n, b);
+            }
+        }
+    }
+    __syncthreads();
     {
         uint32_t *dst = reinterpret_cast<uint32_t *>(btn + T0);
         const int last = min(kTileLeaves, n - 1 - T0);     // internal indices < n-1
-        for (int w = tid; w < last * kRecWords; w += kTileThreads)
-            if (own[w / kRecWords]) dst[w] = rec[w];
+        for (int q = tid; q < last * kRecWords; q += kTileThreads)
+            if (own[q / kRecWords]) dst[q] = rec[q];
     }
-    // ---- climb above the tile (one thread)
+    // ---- climb above the tile (one thread, holding the tile's bound)
     if (tid != 0 || n <= kTileLeaves) return;
-    float b[6];
-    for (int a = 0; a < 6; ++a) b[a] = sb[a * kTileLeaves];
     int level = kTileLog;
     int j = tile;                                          // block index at `level`
     int off = 0;                                           // level_offset(level)
@@ -779,21 +830,17 @@ __device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ a
     }
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict__ aabbs,
-                                                         const int32_t *__restrict__ sorted,
-                                                         int n, ptgpu_bvh_node *__restrict__ btn,
-                                                         ptgpu_bvh_node *__restrict__ btl,
+__global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict__ lb, int n,
+                                                         ptgpu_bvh_node *__restrict__ btn,
                                                          float *__restrict__ block_bounds,
                                                          uint32_t *__restrict__ arrivals, int ntiles) {
     extern __shared__ __align__(16) unsigned char tsm[];
-    emit_tile(blockIdx.x, aabbs, sorted, 0, n, btn, btl, block_bounds, arrivals, ntiles, tsm);
+    emit_tile(blockIdx.x, lb, n, btn, block_bounds, arrivals, ntiles, tsm);
 }
 
 // the tiles of every segment's tree in one launch
-__global__ void __launch_bounds__(kTileThreads) k_tiles_seg(const float4 *__restrict__ aabbs,
-                                                             const int32_t *__restrict__ sorted,
-                                                             SegBuild sb, ptgpu_bvh_node *__restrict__ btn,
-                                                             ptgpu_bvh_node *__restrict__ btl,
+__global__ void __launch_bounds__(kTileThreads) k_tiles_seg(const float4 *__restrict__ lb, SegBuild sb,
+                                                             ptgpu_bvh_node *__restrict__ btn,
                                                              float *__restrict__ block_bounds,
                                                              uint32_t *__restrict__ arrivals) {
     extern __shared__ __align__(16) unsigned char tsm[];
@@ -802,8 +849,8 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles_seg(const float4 *__rest
     const int off = sb.seg_off[g], n = sb.seg_off[g + 1] - off;
     const int tile = t - sb.tile_off[g];
     const int64_t bb = sb.bb_off[g];
-    emit_tile(tile, aabbs, sorted + off, off, n, btn + (off - g), btl + off, block_bounds + 6 * bb,
-              arrivals + bb, sb.tile_off[g + 1] - sb.tile_off[g], tsm);
+    emit_tile(tile, lb + 2 * (size_t)off, n, btn + (off - g), block_bounds + 6 * bb, arrivals + bb,
+              sb.tile_off[g + 1] - sb.tile_off[g], tsm);
 }
 
 // ---------------------------------------------------------------------------
@@ -1338,8 +1385,10 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
         b.keys_tmp, b.vals_tmp, b.keys_alt, b.vals_alt, n, 2, b.state, b.status + 2 * pass_words);
     k_onesweep<false, true><<<ntiles_sort, kSortThreads, smem, s>>>(
         b.keys_alt, b.vals_alt, nullptr, b.sorted, n, 3, b.state, b.status + 3 * pass_words);
-    k_tiles<<<ntiles, kTileThreads, kTileSmem, s>>>(b.aabbs, b.sorted, n, b.btn, b.btl,
-                                                    b.block_bounds, b.arrivals, ntiles);
+    k_leaves<<<(n + kLeafThreads - 1) / kLeafThreads, kLeafThreads, 0, s>>>(b.aabbs, b.sorted, n, nullptr,
+                                                                             0, b.btl, b.leaf_bounds);
+    k_tiles<<<ntiles, kTileThreads, kTileSmem, s>>>(b.leaf_bounds, n, b.btn, b.block_bounds,
+                                                    b.arrivals, ntiles);
     return cudaGetLastError();
 }
 
@@ -1379,8 +1428,10 @@ cudaError_t launch_lbvh_build_seg(const LbvhBuffers &b, int n, const SegBuild &s
         b.keys_alt, b.vals_alt, b.keys_tmp, b.vals_tmp, n, 3, b.state, b.status + 3 * pw);
     k_onesweep<false, true, true><<<ntiles_sort, kSortThreads, smem, s>>>(
         nullptr, b.vals_tmp, nullptr, b.sorted, n, 4, b.state, b.status + 4 * pw, sb.seg_off, sb.n_segs);
-    k_tiles_seg<<<sb.n_tiles, kTileThreads, kTileSmem, s>>>(b.aabbs, b.sorted, sb, b.btn, b.btl,
-                                                            b.block_bounds, b.arrivals);
+    k_leaves<<<(n + kLeafThreads - 1) / kLeafThreads, kLeafThreads, 0, s>>>(b.aabbs, b.sorted, n, sb.seg_off,
+                                                                             sb.n_segs, b.btl, b.leaf_bounds);
+    k_tiles_seg<<<sb.n_tiles, kTileThreads, kTileSmem, s>>>(b.leaf_bounds, sb, b.btn, b.block_bounds,
+                                                            b.arrivals);
     return cudaGetLastError();
 }
 

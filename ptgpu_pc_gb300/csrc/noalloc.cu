@@ -29,9 +29,9 @@ namespace ptgpu {
 
 namespace {
 
-// 24.3 MiB are needed at kNoAllocMaxShapes; the rest is slack
+// 31.8 MiB are needed at kNoAllocMaxShapes; the rest is slack
 constexpr uint32_t kNoAllocMaxShapes = 1u << 18;
-constexpr size_t kNoAllocScratchBytes = size_t(25) << 20;
+constexpr size_t kNoAllocScratchBytes = size_t(33) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -52,6 +52,7 @@ size_t carve(unsigned char *base, size_t n, LbvhBuffers &b) {
     b.verts = reinterpret_cast<float *>(take(n * 9 * sizeof(float)));
     b.type = take(n);
     b.aabbs = reinterpret_cast<float4 *>(take(n * 2 * sizeof(float4)));
+    b.leaf_bounds = reinterpret_cast<float4 *>(take(n * 2 * sizeof(float4)));
     b.keys = reinterpret_cast<uint32_t *>(take(n * 4));
     b.keys_alt = reinterpret_cast<uint32_t *>(take(n * 4));
     b.keys_tmp = reinterpret_cast<uint32_t *>(take(n * 4));
