@@ -46,7 +46,7 @@ extern "C" {
 #define PTGPU_MAX_DEPTH    6
 #define PTGPU_ACCEL_NONE   0   /* ACCELSTR 0: brute force                   */
 #define PTGPU_ACCEL_BVH    1   /* ACCELSTR 1: LBVH (the reference default)  */
-#define PTGPU_ACCEL_KDTREE 2   /* ACCELSTR 2: host-built KD tree            */
+#define PTGPU_ACCEL_KDTREE 2   /* ACCELSTR 2: KD tree (KDTree::build)       */
 
 /* ---- shared geometry types (include/geom.h:48-91, vec.h:27-29) ----------- */
 typedef struct { float x, y, z; } ptgpu_vec;                 /* Vec      */
@@ -121,6 +121,8 @@ typedef struct {
                                          right-to-left (the order g++ gives the
                                          reference source; the default is the
                                          left-to-right order of OpenCL/clang)   */
+#define PTGPU_FLAG_KD_HOST       0x20 /* build the KD tree with the sequential host
+                                         code instead of the GPU (same tree)     */
 /* build flag field: rounds of the treelet stage (bits 8-11; 0 = one round,
  * the single launch of CLBVH::optimize, CLBVH.cpp:318-350).  Each round runs
  * over the tree the previous one left; Karras & Aila use three. */

@@ -104,6 +104,7 @@ FLAG_MORTON_DELTA = 0x2
 FLAG_TREELET = 0x4
 FLAG_ARGS_RTL = 0x8
 FLAG_WIDE_TRAVERSAL = 0x10
+FLAG_KD_HOST = 0x20
 
 
 def treelet_sweeps(n):

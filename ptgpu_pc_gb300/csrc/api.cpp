@@ -99,6 +99,7 @@ struct ptgpu_ctx {
     bool wide = false;
     int32_t root_first = 0, root_count = 0;
     KdTree kd;
+    KdScratch *kd_scratch = nullptr;
     bool kd_valid = false;
     // rendering
     int w = 0, h = 0;
@@ -228,6 +229,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_wf, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
+    kd_scratch_destroy(c->kd_scratch);
     if (c->h_pixels) cudaFreeHost(c->h_pixels);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -441,10 +443,18 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
         c->accel_built = PTGPU_ACCEL_BVH;
         return PTGPU_OK;
     }
-    // KD tree: host build with the reference topology, device traversal
+    // KD tree with the reference topology (on the GPU unless asked for the
+    // host build), device traversal
     auto t0 = std::chrono::steady_clock::now();
-    int st = kd_build(c->h_shapes.data(), c->n, c->kd);
-    if (st) return fail(st, "kd build failed");
+    if (flags & PTGPU_FLAG_KD_HOST) {
+        int st = kd_build(c->h_shapes.data(), c->n, c->kd);
+        if (st) return fail(st, "kd build failed");
+    } else {
+        if (!c->kd_scratch) c->kd_scratch = kd_scratch_create();
+        CK(kd_build_gpu(c->d_verts.as<float>(), c->d_type.as<uint8_t>(), c->n, c->kd, *c->kd_scratch,
+                        c->stream));
+    }
+    int st;
     for (uint32_t i = 0; i < c->n; ++i) { c->h_shapes[i].index = (int32_t)i; c->h_shapes[i].morton_code = 0; }
     std::vector<float> nodes;
     float root_box[6];

@@ -161,6 +161,15 @@ cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int
                                  uint32_t *id, int32_t *hit, cudaStream_t s,
                                  unsigned int *counter = nullptr);
 
+// kd_gpu.cu: the KD tree of KDTree::build on the device, from the build
+// vertices and types; node ids breadth-first (scratch kept between builds)
+struct KdTree;
+struct KdScratch;
+KdScratch *kd_scratch_create();
+void kd_scratch_destroy(KdScratch *w);
+cudaError_t kd_build_gpu(const float *verts, const uint8_t *type, uint32_t n, KdTree &kd, KdScratch &w,
+                         cudaStream_t s);
+
 // host helpers shared by the single-scene API and the batch (api.cpp)
 int record_error(int code, const std::string &msg);
 void make_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
