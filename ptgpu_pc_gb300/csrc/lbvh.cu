@@ -9,13 +9,15 @@
 //                       stable bubble sort, CLBVH.cpp:31-47), 8-bit digits,
 //                       warp-level ranking through shared lane masks,
 //                       decoupled look-back with a bounded spin
-//   k_leaves            leaf records, and the leaves' bounds in sorted order
-//   k_tiles             per 1024-leaf tile: every internal node inside the
-//                       tile, bounds by a warp-shuffle bottom-up reduction,
-//                       then a climb over the tiles for the nodes above them
+//   k_emit              per 256-leaf window: the leaf records, then every
+//                       internal node inside the window, bounds by a
+//                       warp-shuffle bottom-up reduction, then a climb over
+//                       the windows for the nodes above them
 //                       (kernelConstructRadixTree and kernelConstructBVHTree,
 //                       BVH.cl:141-258, with the closed-form topology of
-//                       lbvh_topo.cuh)
+//                       lbvh_topo.cuh).  The batched build runs k_leaves
+//                       (leaf records and the leaves' bounds in sorted order)
+//                       and k_tiles_seg (1024-leaf tiles of every segment).
 // The result is the reference's btn[N-1]/btl[N] arrays, resident on the
 // device.  k_abi_to_trace then derives the 64-byte traversal nodes.
 #include <cfloat>
@@ -380,7 +382,10 @@ __global__ void __launch_bounds__(256) k_seg_morton(const float *__restrict__ ve
 // ---------------------------------------------------------------------------
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 15;
+#ifndef PTGPU_SORT_ITEMS
+#define PTGPU_SORT_ITEMS 15
+#endif
+constexpr int kSortItems = PTGPU_SORT_ITEMS;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1u;
 constexpr int kSpinLimit = 1 << 22;
@@ -650,11 +655,46 @@ __device__ __forceinline__ BlockNode block_node(int lo, int hi, int level, int n
     return r;
 }
 
-// offset of level `level` (>= kTileLog) in the per-level block arrays
-__device__ __forceinline__ int level_offset(int level, int ntiles) {
-    int off = 0;
-    for (int l = kTileLog; l < level; ++l) off += (ntiles + (1 << (l - kTileLog)) - 1) >> (l - kTileLog);
-    return off;
+// The nodes above the blocks of 2^base_log leaves that one CTA emits: the
+// block's bound goes to a per-level array, and of the two blocks under a
+// parent the one that arrives second merges them, writes the parent's record
+// and moves up.  `j` is the CTA's block, `b` its bound; per-level arrays are
+// laid out level after level (nblocks, then ceil(nblocks/2), ...).
+__device__ __forceinline__ void climb_blocks(int base_log, int j, float b[6], int n,
+                                             ptgpu_bvh_node *__restrict__ btn,
+                                             float *__restrict__ block_bounds,
+                                             uint32_t *__restrict__ arrivals, int nblocks) {
+    int level = base_log;
+    int off = 0;                                           // first block of `level`
+    for (;;) {
+        float *mine = block_bounds + 6 * (size_t)(off + j);
+        for (int a = 0; a < 6; ++a) mine[a] = b[a];
+        if ((1 << level) >= n) break;                      // this block is the root's
+        const int noff = off + ((nblocks + (1 << (level - base_log)) - 1) >> (level - base_log));
+        const int pj = j >> 1;
+        const int64_t right_lo = ((int64_t)(2 * pj + 1)) << level;
+        if (right_lo >= n) {                               // parent has no right half
+            level++; j = pj; off = noff;
+            continue;
+        }
+        __threadfence();
+        if (atomicAdd(&arrivals[noff + pj], 1u) == 0u) return;   // sibling not done yet
+        __threadfence();
+        const float *lbp = block_bounds + 6 * (size_t)(off + 2 * pj);
+        const float *rbp = block_bounds + 6 * (size_t)(off + 2 * pj + 1);
+        for (int a = 0; a < 6; ++a) b[a] = __ldcg(lbp + a);
+        float c[6];
+        for (int a = 0; a < 6; ++a) c[a] = __ldcg(rbp + a);
+        merge6(b, c);
+        level++;
+        const int lo = (int)((int64_t)pj << level);
+        const int64_t he = (int64_t)lo + ((int64_t)1 << level);
+        const int hi = (int)((he < n ? he : n) - 1);
+        const BlockNode bn = block_node(lo, hi, level, n);
+        write_node(&btn[bn.idx], lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
+        j = pj;
+        off = noff;
+    }
 }
 
 // Leaf records of every tree, and the leaves' bounds in sorted order for the
@@ -709,13 +749,14 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaves(const float4 *__restric
 // bound.  Records are staged in shared memory (the active lanes of a level
 // are 2^(L-1) apart, so a staging store meets at most two lanes per bank)
 // and copied out as coalesced words.
+template <int kSpan>
 __device__ __forceinline__ void block_record(uint32_t *rec, unsigned char *own, int T0, int l0,
                                              int level, int n, const float b[6]) {
     const int lo = T0 + l0;
     const int hi = min(T0 + l0 + (1 << level), n) - 1;
     const BlockNode bn = block_node(lo, hi, level, n);
     const int j = bn.idx - T0;
-    if (bn.idx >= 0 && bn.idx < n - 1 && j >= 0 && j < kTileLeaves) {   // internal, in the tile
+    if (bn.idx >= 0 && bn.idx < n - 1 && j >= 0 && j < kSpan) {         // internal, in the window
         stage_node(rec + j * kRecWords, lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
         own[j] = 1;
     }
@@ -755,7 +796,7 @@ __device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ l
         }
     }
     __syncthreads();                                // own[] cleared
-    if (have && l0 + 1 < cnt) block_record(rec, own, T0, l0, 1, n, b);
+    if (have && l0 + 1 < cnt) block_record<kTileLeaves>(rec, own, T0, l0, 1, n, b);
     // ---- levels 2-6 inside the warp
 #pragma unroll
     for (int level = 2; level <= 6; ++level) {
@@ -764,7 +805,7 @@ __device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ l
         const bool leader = (lane & ((off << 1) - 1)) == 0;
         if (leader && have && l0 + (1 << (level - 1)) < cnt) {
             merge6(b, c);
-            block_record(rec, own, T0, l0, level, n, b);
+            block_record<kTileLeaves>(rec, own, T0, l0, level, n, b);
         }
     }
     if (lane == 0 && have)
@@ -783,7 +824,7 @@ __device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ l
             const bool leader = (lane & ((off << 1) - 1)) == 0;
             if (leader && have && wl0 + (1 << (level - 1)) < cnt) {
                 merge6(b, c);
-                block_record(rec, own, T0, wl0, level, n, b);
+                block_record<kTileLeaves>(rec, own, T0, wl0, level, n, b);
             }
         }
     }
@@ -796,38 +837,7 @@ __device__ __forceinline__ void emit_tile(int tile, const float4 *__restrict__ l
     }
     // ---- climb above the tile (one thread, holding the tile's bound)
     if (tid != 0 || n <= kTileLeaves) return;
-    int level = kTileLog;
-    int j = tile;                                          // block index at `level`
-    int off = 0;                                           // level_offset(level)
-    for (;;) {
-        float *mine = block_bounds + 6 * (size_t)(off + j);
-        for (int a = 0; a < 6; ++a) mine[a] = b[a];
-        if ((1 << level) >= n) break;                      // this block is the root's
-        const int noff = off + ((ntiles + (1 << (level - kTileLog)) - 1) >> (level - kTileLog));
-        const int pj = j >> 1;
-        const int64_t right_lo = ((int64_t)(2 * pj + 1)) << level;
-        if (right_lo >= n) {                               // parent has no right half
-            level++; j = pj; off = noff;
-            continue;
-        }
-        __threadfence();
-        if (atomicAdd(&arrivals[noff + pj], 1u) == 0u) return;   // sibling not done yet
-        __threadfence();
-        const float *lb = block_bounds + 6 * (size_t)(off + 2 * pj);
-        const float *rb = block_bounds + 6 * (size_t)(off + 2 * pj + 1);
-        for (int a = 0; a < 6; ++a) b[a] = __ldcg(lb + a);
-        float c[6];
-        for (int a = 0; a < 6; ++a) c[a] = __ldcg(rb + a);
-        merge6(b, c);
-        level++;
-        const int lo = (int)((int64_t)pj << level);
-        const int64_t he = (int64_t)lo + ((int64_t)1 << level);
-        const int hi = (int)((he < n ? he : n) - 1);
-        const BlockNode bn = block_node(lo, hi, level, n);
-        write_node(&btn[bn.idx], lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
-        j = pj;
-        off = noff;
-    }
+    climb_blocks(kTileLog, tile, b, n, btn, block_bounds, arrivals, ntiles);
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict__ lb, int n,
@@ -836,6 +846,92 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict
                                                          uint32_t *__restrict__ arrivals, int ntiles) {
     extern __shared__ __align__(16) unsigned char tsm[];
     emit_tile(blockIdx.x, lb, n, btn, block_bounds, arrivals, ntiles, tsm);
+}
+
+// Single-tree emission in one pass (the batched build keeps k_leaves +
+// k_tiles_seg).  A CTA of 256 threads owns the 256 leaves [k0, k0 + 255]:
+// each thread gathers its sorted shape's 32-byte bound and stages the leaf
+// record; the records leave as coalesced words.  The bounds stay in
+// registers for the internal nodes inside the window -- the blocks of 2^L
+// leaves at L = 1..5 by warp shuffles (a block merges with its right half,
+// 2^(L-1) lanes up), L = 6..8 in warp 0 over the 8 warps' bounds -- whose
+// records (numbered lo or hi, so inside [k0, k0 + 255]) are staged in the
+// same buffer and copied out where the window owns them.  Thread 0 then
+// climbs above the window with the block's bound.  Against k_leaves +
+// k_tiles this writes and re-reads no leaf-order bound array.
+constexpr int kEmitLog = 8;
+constexpr int kEmitLeaves = 1 << kEmitLog;
+static_assert(kEmitLeaves == kLeafThreads, "one leaf per thread");
+__global__ void __launch_bounds__(kLeafThreads) k_emit(const float4 *__restrict__ aabbs,
+                                                        const int32_t *__restrict__ sorted, int n,
+                                                        ptgpu_bvh_node *__restrict__ btl,
+                                                        ptgpu_bvh_node *__restrict__ btn,
+                                                        float *__restrict__ block_bounds,
+                                                        uint32_t *__restrict__ arrivals, int nblocks) {
+    __shared__ uint32_t rec[kEmitLeaves * kRecWords];
+    __shared__ float wb[8 * 6];
+    __shared__ unsigned char own[kEmitLeaves];
+    const int k0 = blockIdx.x * kEmitLeaves;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int cnt = min(kEmitLeaves, n - k0);
+    const bool have = tid < cnt;
+    float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, c[6];
+    own[tid] = 0;
+    if (have) {
+        const int k = k0 + tid;
+        const int sh = min(max(__ldg(sorted + k), 0), n - 1);     // in bounds even after a failed sort
+        const float4 q0 = __ldg(aabbs + 2 * (size_t)sh), q1 = __ldg(aabbs + 2 * (size_t)sh + 1);
+        b[0] = q0.x; b[1] = q0.y; b[2] = q0.z; b[3] = q0.w; b[4] = q1.x; b[5] = q1.y;
+        const int parent = n >= 2 ? topo_parent_leaf(k, n) : -1;
+        stage_node(rec + tid * kRecWords, -1, -1, sh, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
+    }
+    __syncthreads();
+    {
+        uint32_t *dst = reinterpret_cast<uint32_t *>(btl + k0);
+        for (int q = tid; q < cnt * kRecWords; q += kLeafThreads) dst[q] = rec[q];
+    }
+    __syncthreads();                                // staging buffer free, own[] cleared
+    // ---- levels 1-5 inside the warp
+#pragma unroll
+    for (int level = 1; level <= 5; ++level) {
+        const int off = 1 << (level - 1);           // lanes between a block's halves
+        shfl_down6(c, b, off);
+        const bool leader = (lane & ((off << 1) - 1)) == 0;
+        if (leader && have && tid + off < cnt) {
+            merge6(b, c);
+            block_record<kEmitLeaves>(rec, own, k0, tid, level, n, b);
+        }
+    }
+    if (lane == 0 && have)
+        for (int a = 0; a < 6; ++a) wb[w * 6 + a] = b[a];
+    __syncthreads();
+    // ---- levels 6-8 over the 8 warps, in warp 0
+    if (w == 0) {
+        const int wl0 = 32 * lane;                  // lane j holds warp j's block
+        const bool h = lane < 8 && wl0 < cnt;
+        if (h)
+            for (int a = 0; a < 6; ++a) b[a] = wb[lane * 6 + a];
+#pragma unroll
+        for (int level = 6; level <= 8; ++level) {
+            const int off = 1 << (level - 6);
+            shfl_down6(c, b, off);
+            const bool leader = (lane & ((off << 1) - 1)) == 0;
+            if (leader && h && wl0 + (1 << (level - 1)) < cnt) {
+                merge6(b, c);
+                block_record<kEmitLeaves>(rec, own, k0, wl0, level, n, b);
+            }
+        }
+    }
+    __syncthreads();
+    {
+        uint32_t *dst = reinterpret_cast<uint32_t *>(btn + k0);
+        const int last = min(kEmitLeaves, n - 1 - k0);     // internal indices < n-1
+        for (int q = tid; q < last * kRecWords; q += kLeafThreads)
+            if (own[q / kRecWords]) dst[q] = rec[q];
+    }
+    // ---- climb above the window (thread 0 holds the window's bound)
+    if (tid != 0 || n <= kEmitLeaves) return;
+    climb_blocks(kEmitLog, blockIdx.x, b, n, btn, block_bounds, arrivals, nblocks);
 }
 
 // the tiles of every segment's tree in one launch
@@ -1330,9 +1426,12 @@ size_t sort_status_words(int n) {
     return tiles * 256 * 5;
 }
 
+// per-level block bounds above the emission windows: 256-leaf windows in the
+// single-tree build (k_emit), 1024-leaf tiles in the batched one -- the
+// former needs more, so both size by it
 size_t block_bound_count(int n) {
-    size_t ntiles = ((size_t)n + kTileLeaves - 1) / kTileLeaves;
-    return 2 * ntiles + 64;
+    const size_t nblocks = ((size_t)n + kEmitLeaves - 1) / kEmitLeaves;
+    return 2 * nblocks + 64;
 }
 
 template <class K> static void sort_attrs(K k, size_t smem) {
@@ -1362,7 +1461,7 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
                               cudaStream_t s) {
     if (n < 1) return cudaErrorInvalidValue;
     const int ntiles_sort = (n + kSortTile - 1) / kSortTile;
-    const int ntiles = (n + kTileLeaves - 1) / kTileLeaves;
+    const int nblocks = (n + kEmitLeaves - 1) / kEmitLeaves;
     cudaError_t e = launch_lbvh_prepare_attrs();
     if (e != cudaSuccess) return e;
     const size_t smem = sizeof(SortSmem);
@@ -1385,10 +1484,8 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
         b.keys_tmp, b.vals_tmp, b.keys_alt, b.vals_alt, n, 2, b.state, b.status + 2 * pass_words);
     k_onesweep<false, true><<<ntiles_sort, kSortThreads, smem, s>>>(
         b.keys_alt, b.vals_alt, nullptr, b.sorted, n, 3, b.state, b.status + 3 * pass_words);
-    k_leaves<<<(n + kLeafThreads - 1) / kLeafThreads, kLeafThreads, 0, s>>>(b.aabbs, b.sorted, n, nullptr,
-                                                                             0, b.btl, b.leaf_bounds);
-    k_tiles<<<ntiles, kTileThreads, kTileSmem, s>>>(b.leaf_bounds, n, b.btn, b.block_bounds,
-                                                    b.arrivals, ntiles);
+    k_emit<<<nblocks, kLeafThreads, 0, s>>>(b.aabbs, b.sorted, n, b.btl, b.btn, b.block_bounds, b.arrivals,
+                                            nblocks);
     return cudaGetLastError();
 }
 
