@@ -123,4 +123,37 @@ __host__ __device__ __forceinline__ int32_t topo_parent_leaf(int32_t k, int32_t 
     return k - 1;
 }
 
+// Record fields of the node covering the block [lo, hi] = [j*2^L, ...] at
+// level L (both halves non-empty): its index, split, parent and leaf flag.
+struct TopoBlock { int32_t idx, gamma, parent, leaf; };
+__host__ __device__ __forceinline__ TopoBlock topo_block(int32_t lo, int32_t hi, int level, int32_t n) {
+    int32_t a_lo, a_hi, a_g;
+    topo_range(lo, n, a_lo, a_hi, a_g);
+    TopoBlock r;
+    r.idx = (a_lo == lo && a_hi == hi) ? lo : hi;
+    r.gamma = lo + (1 << (level - 1)) - 1;
+    r.leaf = (level == 1 || hi == r.gamma + 1) ? 2 : 0;
+    r.parent = topo_parent_internal(r.idx, lo, hi, n);
+    return r;
+}
+
+// The same fields in a few integer operations for a block away from the
+// right edge and the root: the block is complete, its sibling exists (so it
+// is its parent's left child, numbered by its end, or right child, numbered
+// by its start), and its parent's sibling exists (so the parent is numbered
+// the same way one level up).  Other blocks take topo_block.
+__host__ __device__ __forceinline__ TopoBlock topo_block_fast(int32_t lo, int32_t hi, int level, int32_t n) {
+    const int32_t j = lo >> level, jp = j >> 1;
+    const bool fast = ((int64_t)(j + 1) << level) <= n && ((int64_t)(j ^ 1) << level) < n &&
+                      ((int64_t)(jp ^ 1) << (level + 1)) < n;
+    if (!fast) return topo_block(lo, hi, level, n);
+    TopoBlock r;
+    r.idx = (j & 1) ? lo : hi;
+    r.gamma = lo + (1 << (level - 1)) - 1;
+    r.leaf = level == 1 ? 2 : 0;
+    const int32_t plo = jp << (level + 1);
+    r.parent = (jp & 1) ? plo : plo + (2 << level) - 1;
+    return r;
+}
+
 }  // namespace ptgpu

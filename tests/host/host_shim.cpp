@@ -1,6 +1,8 @@
 // host_shim.cpp -- test-only C entry points over the library's host code
 // (KD-tree build, scene loader, camera, closed-form LBVH topology), compiled
 // without CUDA by the CPU tests.
+#include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -21,6 +23,26 @@ void shim_topology(int n, int *mn, int *mx, int *gamma, int *parent, int *leaf, 
         leaf[i] = (t.left_leaf || t.right_leaf) ? 2 : 0;
     }
     for (int k = 0; k < n; ++k) leaf_parent[k] = ptgpu::topo_parent_leaf(k, n);
+}
+
+// Every block of 2^L leaves with both halves non-empty: the short form of its
+// record fields against the general one, and the general one against the
+// node that carries its index.  Returns the number of mismatches.
+int shim_check_blocks(int n) {
+    int bad = 0;
+    for (int level = 1; level < 31 && (1 << (level - 1)) < n; ++level) {
+        for (int64_t lo = 0; lo < n; lo += (int64_t)1 << level) {
+            if (lo + ((int64_t)1 << (level - 1)) >= n) continue;          // right half empty
+            const int hi = (int)std::min<int64_t>(lo + ((int64_t)1 << level), n) - 1;
+            const ptgpu::TopoBlock g = ptgpu::topo_block((int)lo, hi, level, n);
+            const ptgpu::TopoBlock f = ptgpu::topo_block_fast((int)lo, hi, level, n);
+            if (g.idx != f.idx || g.gamma != f.gamma || g.parent != f.parent || g.leaf != f.leaf) ++bad;
+            const ptgpu::TopoNode t = ptgpu::topo_node(g.idx, n);
+            const int leaf = (t.left_leaf || t.right_leaf) ? 2 : 0;
+            if (t.lo != (int)lo || t.hi != hi || t.gamma != g.gamma || t.parent != g.parent || leaf != g.leaf) ++bad;
+        }
+    }
+    return bad;
 }
 
 static ptgpu::KdTree g_kd;

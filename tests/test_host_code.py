@@ -25,6 +25,7 @@ def shim(tmp_path_factory):
     L = ctypes.CDLL(out)
     vp = ctypes.c_void_p
     L.shim_topology.argtypes = [ctypes.c_int] + [vp] * 6
+    L.shim_check_blocks.argtypes = [ctypes.c_int]
     L.shim_kd_build.argtypes = [vp, ctypes.c_int, vp, vp, vp]
     L.shim_kd_export.argtypes = [vp, ctypes.c_int64, vp]
     L.shim_read_scene.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp,
@@ -49,6 +50,13 @@ def test_closed_form_topology(n, shim, orc):
     assert np.array_equal(g, btn["nLeft"]) and np.array_equal(g + 1, btn["nRight"])
     assert np.array_equal(par, btn["nParent"]) and np.array_equal(leaf, btn["leaf"])
     assert np.array_equal(lp, btl["nParent"])
+
+
+def test_block_fields_short_form(shim):
+    """The emission kernels' short form of a block's record fields equals the
+    general closed form, which equals the node carrying the block's index."""
+    for n in list(range(2, 1100)) + [4095, 4096, 4097, 81934, 100003, 262144, 262145, 4194304]:
+        assert shim.shim_check_blocks(n) == 0, n
 
 
 @pytest.mark.parametrize("case", ["cornell", "ico2", "ico4", "soup"])
