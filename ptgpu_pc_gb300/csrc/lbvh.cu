@@ -503,13 +503,17 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     if (tid == 0) { sm.tile = (int)atomicAdd(&st->tile_counter[pass], 1u); sm.abort = 0; }
     if (SEG)
         for (int i = tid; i <= n_segs; i += kSortThreads) sm.seg_off[i] = seg_off[i];
-    for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&sm.warp_hist[0][0])[i] = 0u;
-    for (int i = tid; i < 2 * kSortWarps * 256; i += kSortThreads) (&sm.u.match[0][0][0])[i] = 0u;
+    static_assert(kSortWarps * 256 % (4 * kSortThreads) == 0, "16-byte clears");
+    const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = tid; i < kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.warp_hist[0][0])[i] = zero4;
+    for (int i = tid; i < 2 * kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.u.match[0][0][0])[i] = zero4;
     // global digit offsets for this pass
     uint32_t gcount = st->hist[pass][tid];
     uint32_t goff = block_excl_scan256(gcount, sm.scan_tmp);
     __syncthreads();
     const int tile = sm.tile;
+    // 64-bit positions: measured faster here than 32-bit ones (4M keys: 4 passes
+    // 0.148 -> 0.183 ms with int)
     const int64_t base = (int64_t)tile * kSortTile;
     uint32_t key[kSortItems];
     int32_t val[kSortItems];
@@ -531,7 +535,7 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     }
 #pragma unroll
     for (int j = 0; j < kSortItems; ++j) {
-        const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
+        const int idx = base + w * 32 * kSortItems + j * 32 + lane;
         const bool valid = idx < n;
         uint32_t dig = (key[j] >> shift) & 255u;
         // lanes with the same digit: each sets its bit in the digit's mask
@@ -600,7 +604,7 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
         if (timed_out) { atomicOr(&st->error, 1u); sm.abort = 1; }
         st_volatile(my, kFlagInc | ((excl + count) & kValMask));
     }
-    sm.tile_excl[tid] = goff + excl;
+    sm.tile_excl[tid] = goff + excl - dstart;       // + tile position = destination (mod 2^32)
     __syncthreads();
     // scatter into shared memory in tile-sorted order
 #pragma unroll
@@ -614,11 +618,11 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     }
     __syncthreads();
     if (sm.abort) return;
-    const int valid_cnt = (int)min((int64_t)kSortTile, (int64_t)n - base);
+    const int valid_cnt = (int)min((int64_t)kSortTile, (int64_t)n - (int64_t)base);
     for (int i = tid; i < valid_cnt; i += kSortThreads) {
         uint32_t k = sm.u.st.keys[i];
         uint32_t dig = (k >> shift) & 255u;
-        uint32_t dest = sm.tile_excl[dig] + ((uint32_t)i - sm.digit_start[dig]);
+        uint32_t dest = sm.tile_excl[dig] + (uint32_t)i;
         if (dest < (uint32_t)n) {
             if (!LAST) keys_out[dest] = k;
             vals_out[dest] = sm.u.st.vals[i];
@@ -863,104 +867,227 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(const float4 *__restrict
     emit_tile(blockIdx.x, lb, n, btn, block_bounds, arrivals, ntiles, tsm);
 }
 
-// Single-tree emission in one pass (the batched build keeps k_leaves +
-// k_tiles_seg).  A CTA of 256 threads owns the 256 leaves [k0, k0 + 255]:
-// each thread gathers its sorted shape's 32-byte bound and stages the leaf
-// record; the records leave as coalesced words.  The bounds stay in
-// registers for the internal nodes inside the window -- the blocks of 2^L
-// leaves at L = 1..5 by warp shuffles (a block merges with its right half,
-// 2^(L-1) lanes up), L = 6..8 in warp 0 over the 8 warps' bounds -- whose
-// records (numbered lo or hi, so inside [k0, k0 + 255]) are staged in the
-// same buffer and copied out where the window owns them.  Thread 0 then
-// climbs above the window with the block's bound.  Against k_leaves +
-// k_tiles this writes and re-reads no leaf-order bound array.
+// Single-tree emission (the batched build keeps k_leaves + k_tiles_seg).
+// k_emit: persistent CTAs of 256 threads walk the 256-leaf windows
+// [k0, k0 + 255].  Each thread gathers its sorted shape's 32-byte bound and
+// stages the leaf record; the records leave as coalesced 16-byte words.  The
+// bounds stay in registers for the internal nodes inside the window -- the
+// blocks of 2^L leaves at L = 1..5 by warp shuffles (a block merges with its
+// right half, 2^(L-1) lanes up), L = 6..8 in warp 0 over the 8 warps'
+// bounds.  The level 1-5 nodes of a warp (31 of them) are then built one per
+// lane from their bounds, parked in shared memory, so the topology and the
+// record staging run on all lanes instead of one leader per block.  Their
+// records are numbered lo or hi, so inside [k0, k0 + 255], and are copied
+// out where the window owns them.  The next window's gather is issued
+// before the current window is emitted, so every CTA keeps loads in flight.
+// The window's bound goes to win_bounds.  k_emit_upper then does the same
+// over the windows (levels 9-16, one CTA per 256 windows) and climbs above.
+#ifndef PTGPU_EMIT_MINBLOCKS
+#define PTGPU_EMIT_MINBLOCKS 6
+#endif
 constexpr int kEmitLog = 8;
 constexpr int kEmitLeaves = 1 << kEmitLog;
+constexpr int kUpperLog = 2 * kEmitLog;          // leaves under one k_emit_upper CTA
 static_assert(kEmitLeaves == kLeafThreads, "one leaf per thread");
-__global__ void __launch_bounds__(kLeafThreads, 8) k_emit(const float4 *__restrict__ aabbs,
+
+__device__ __forceinline__ void gather_bound(const float4 *__restrict__ aabbs,
+                                             const int32_t *__restrict__ sorted, int k, int n,
+                                             int &sh, float4 &q0, float4 &q1) {
+    sh = min(max(__ldg(sorted + k), 0), n - 1);                 // in bounds even after a failed sort
+    q0 = __ldg(aabbs + 2 * (size_t)sh);
+    q1 = __ldg(aabbs + 2 * (size_t)sh + 1);
+}
+
+__global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(const float4 *__restrict__ aabbs,
                                                         const int32_t *__restrict__ sorted, int n,
                                                         ptgpu_bvh_node *__restrict__ btl,
                                                         ptgpu_bvh_node *__restrict__ btn,
-                                                        float *__restrict__ block_bounds,
-                                                        uint32_t *__restrict__ arrivals, int nblocks) {
+                                                        float *__restrict__ win_bounds, int nblocks) {
     pdl_begin();
     __shared__ __align__(16) uint32_t rec[kEmitLeaves * kRecWords];
+    __shared__ float slot_b[8][32 * 7];     // per warp: the bounds of its 31 nodes, 7 floats apart
     __shared__ float wb[8 * 6];
     __shared__ unsigned char own[kEmitLeaves];
-    const int k0 = blockIdx.x * kEmitLeaves;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int cnt = min(kEmitLeaves, n - k0);
-    const bool have = tid < cnt;
-    float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, c[6];
-    own[tid] = 0;
-    if (have) {
-        const int k = k0 + tid;
-        const int sh = min(max(__ldg(sorted + k), 0), n - 1);     // in bounds even after a failed sort
-        const float4 q0 = __ldg(aabbs + 2 * (size_t)sh), q1 = __ldg(aabbs + 2 * (size_t)sh + 1);
-        b[0] = q0.x; b[1] = q0.y; b[2] = q0.z; b[3] = q0.w; b[4] = q1.x; b[5] = q1.y;
-        const int parent = n >= 2 ? topo_parent_leaf(k, n) : -1;
-        stage_node(rec + tid * kRecWords, -1, -1, sh, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
-    }
-    __syncthreads();
-    {   // the window's records start on a 16-byte boundary (256 * 60 bytes per window)
-        uint32_t *dst = reinterpret_cast<uint32_t *>(btl + k0);
-        const int words = cnt * kRecWords, chunks = words >> 2;
-        for (int c = tid; c < chunks; c += kLeafThreads)
-            reinterpret_cast<uint4 *>(dst)[c] = reinterpret_cast<const uint4 *>(rec)[c];
-        for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) dst[q] = rec[q];
-    }
-    __syncthreads();                                // staging buffer free, own[] cleared
-    // ---- levels 1-5 inside the warp
+    float *sb = slot_b[w];
+    int win = blockIdx.x;
+    int sh = 0;
+    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+    if (win < nblocks && win * kEmitLeaves + tid < n) gather_bound(aabbs, sorted, win * kEmitLeaves + tid, n, sh, q0, q1);
+    for (; win < nblocks; win += gridDim.x) {
+        const int k0 = win * kEmitLeaves;
+        const int cnt = min(kEmitLeaves, n - k0);
+        const bool have = tid < cnt;
+        const int kn = (win + (int)gridDim.x) * kEmitLeaves + tid;
+        const bool have_n = win + (int)gridDim.x < nblocks && kn < n;
+        float b[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y}, c[6];
+        own[tid] = 0;
+        if (have) {
+            const int parent = n >= 2 ? topo_parent_leaf(k0 + tid, n) : -1;
+            stage_node(rec + tid * kRecWords, -1, -1, sh, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
+        }
+        // ---- levels 1-5 inside the warp; level L parks its bounds in
+        // slots 32 - 2^(6-L) ...
 #pragma unroll
-    for (int level = 1; level <= 5; ++level) {
-        const int off = 1 << (level - 1);           // lanes between a block's halves
+        for (int level = 1; level <= 5; ++level) {
+            const int off = 1 << (level - 1);
+            shfl_down6(c, b, off);
+            const bool leader = (lane & ((off << 1) - 1)) == 0;
+            if (leader && have && tid + off < cnt) {
+                merge6(b, c);
+                const int slot = 32 - (64 >> level) + (lane >> level);
+#pragma unroll
+                for (int a = 0; a < 6; ++a) sb[slot * 7 + a] = b[a];
+            }
+        }
+        if (lane == 0 && have)
+            for (int a = 0; a < 6; ++a) wb[w * 6 + a] = b[a];
+        __syncthreads();
+        // ---- the next window's gather, in flight while this one is emitted
+        if (have_n) gather_bound(aabbs, sorted, kn, n, sh, q0, q1);
+        {   // the window's records start on a 16-byte boundary (256 * 60 bytes per window)
+            uint32_t *dst = reinterpret_cast<uint32_t *>(btl + k0);
+            const int words = cnt * kRecWords, chunks = words >> 2;
+            for (int q = tid; q < chunks; q += kLeafThreads)
+                reinterpret_cast<uint4 *>(dst)[q] = reinterpret_cast<const uint4 *>(rec)[q];
+            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) dst[q] = rec[q];
+        }
+        __syncthreads();                            // staging buffer free
+        // ---- the warp's level 1-5 nodes, one per lane (lane 31 idle)
+        if (lane < 31) {
+            const int level = 6 - (32 - __clz(31 - lane));           // 6 - ceil(log2(32 - lane))
+            const int lo_w = (lane - (32 - (64 >> level))) << level;  // first leaf in the warp
+            if (32 * w + lo_w + (1 << (level - 1)) < cnt) {          // right half non-empty
+                float nb[6];
+#pragma unroll
+                for (int a = 0; a < 6; ++a) nb[a] = sb[lane * 7 + a];
+                block_record<kEmitLeaves>(rec, own, k0, 32 * w + lo_w, level, n, nb);
+            }
+        }
+        // ---- levels 6-8 over the 8 warps, in warp 0
+        if (w == 0) {
+            const int wl0 = 32 * lane;              // lane j holds warp j's block
+            const bool h = lane < 8 && wl0 < cnt;
+            if (h)
+                for (int a = 0; a < 6; ++a) b[a] = wb[lane * 6 + a];
+#pragma unroll
+            for (int level = 6; level <= 8; ++level) {
+                const int off = 1 << (level - 6);
+                shfl_down6(c, b, off);
+                const bool leader = (lane & ((off << 1) - 1)) == 0;
+                if (leader && h && wl0 + (1 << (level - 1)) < cnt) {
+                    merge6(b, c);
+                    block_record<kEmitLeaves>(rec, own, k0, wl0, level, n, b);
+                }
+            }
+            if (lane == 0)
+                for (int a = 0; a < 6; ++a) win_bounds[6 * (size_t)win + a] = b[a];
+        }
+        __syncthreads();
+        {   // 16-byte chunks whose records the window owns; words elsewhere
+            uint32_t *dst = reinterpret_cast<uint32_t *>(btn + k0);
+            const int last = min(kEmitLeaves, n - 1 - k0);     // internal indices < n-1
+            const int words = max(last, 0) * kRecWords, chunks = words >> 2;
+            for (int q = tid; q < chunks; q += kLeafThreads) {
+                const int r0 = (4 * q) / kRecWords, r1 = (4 * q + 3) / kRecWords;
+                if (own[r0] && own[r1]) {
+                    reinterpret_cast<uint4 *>(dst)[q] = reinterpret_cast<const uint4 *>(rec)[q];
+                } else {
+                    for (int x = 4 * q; x < 4 * q + 4; ++x)
+                        if (own[x / kRecWords]) dst[x] = rec[x];
+                }
+            }
+            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads)
+                if (own[q / kRecWords]) dst[q] = rec[q];
+        }
+        __syncthreads();                            // rec, own and the slots are reused
+    }
+}
+
+// record of the block at `level` starting at leaf lo, written in place
+__device__ __forceinline__ void upper_record(int lo, int level, int n, const float b[6],
+                                             ptgpu_bvh_node *__restrict__ btn) {
+    const int hi = (int)min((int64_t)lo + ((int64_t)1 << level), (int64_t)n) - 1;
+    const TopoBlock bn = topo_block_fast(lo, hi, level, n);
+    if (bn.idx >= 0 && bn.idx < n - 1)
+        write_node(&btn[bn.idx], lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
+}
+
+// Levels base+1 .. base+8 over 256 units of 2^base leaves each (unit u0 +
+// thread), their bounds in b: levels base+1..base+5 by warp shuffles, the
+// rest in warp 0 over the 8 warps' bounds; records written in place.  On
+// return thread 0 holds the bound of all 256 units.
+__device__ __forceinline__ void reduce_units(float b[6], int u0, int nunits, int base, int n,
+                                             ptgpu_bvh_node *__restrict__ btn, float *wb) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int u = u0 + tid;
+    const bool have = u < nunits;
+    float c[6];
+#pragma unroll
+    for (int m = 1; m <= 5; ++m) {
+        const int off = 1 << (m - 1);
         shfl_down6(c, b, off);
         const bool leader = (lane & ((off << 1) - 1)) == 0;
-        if (leader && have && tid + off < cnt) {
+        if (leader && have && u + off < nunits) {
             merge6(b, c);
-            block_record<kEmitLeaves>(rec, own, k0, tid, level, n, b);
+            upper_record(u << base, base + m, n, b, btn);
         }
     }
     if (lane == 0 && have)
         for (int a = 0; a < 6; ++a) wb[w * 6 + a] = b[a];
     __syncthreads();
-    // ---- levels 6-8 over the 8 warps, in warp 0
     if (w == 0) {
-        const int wl0 = 32 * lane;                  // lane j holds warp j's block
-        const bool h = lane < 8 && wl0 < cnt;
+        const int ul = u0 + 32 * lane;              // lane j holds warp j's 32 units
+        const bool h = lane < 8 && ul < nunits;
         if (h)
             for (int a = 0; a < 6; ++a) b[a] = wb[lane * 6 + a];
 #pragma unroll
-        for (int level = 6; level <= 8; ++level) {
-            const int off = 1 << (level - 6);
+        for (int m = 6; m <= 8; ++m) {
+            const int off = 1 << (m - 6);
             shfl_down6(c, b, off);
             const bool leader = (lane & ((off << 1) - 1)) == 0;
-            if (leader && h && wl0 + (1 << (level - 1)) < cnt) {
+            if (leader && h && ul + (1 << (m - 1)) < nunits) {
                 merge6(b, c);
-                block_record<kEmitLeaves>(rec, own, k0, wl0, level, n, b);
+                upper_record(ul << base, base + m, n, b, btn);
             }
         }
+    }
+}
+
+// The nodes above the windows: one CTA per 256 windows (2^16 leaves) builds
+// levels 9-16 from the window bounds.  Up to 256 such CTAs (2^24 leaves),
+// the CTA that finishes last builds levels 17-24 from their bounds the same
+// way; above that each CTA climbs with arrival counters.
+__global__ void __launch_bounds__(256) k_emit_upper(const float *__restrict__ win_bounds, int nblocks, int n,
+                                                    ptgpu_bvh_node *__restrict__ btn,
+                                                    float *__restrict__ super_bounds,
+                                                    uint32_t *__restrict__ arrivals, int nsuper) {
+    pdl_begin();
+    __shared__ float wb[8 * 6];
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    const int u0 = blockIdx.x * 256;
+    float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (u0 + tid < nblocks)
+        for (int a = 0; a < 6; ++a) b[a] = win_bounds[6 * (size_t)(u0 + tid) + a];
+    reduce_units(b, u0, nblocks, kEmitLog, n, btn, wb);
+    if (n <= (1 << kUpperLog)) return;              // the root was built above
+    if (nsuper > 256) {
+        if (tid == 0) climb_blocks(kUpperLog, blockIdx.x, b, n, btn, super_bounds, arrivals, nsuper);
+        return;
+    }
+    if (tid == 0) {
+        for (int a = 0; a < 6; ++a) super_bounds[6 * (size_t)blockIdx.x + a] = b[a];
+        __threadfence();
+        s_last = atomicAdd(&arrivals[0], 1u) == (uint32_t)(nsuper - 1);
     }
     __syncthreads();
-    {   // 16-byte chunks whose records the window owns; words elsewhere
-        uint32_t *dst = reinterpret_cast<uint32_t *>(btn + k0);
-        const int last = min(kEmitLeaves, n - 1 - k0);     // internal indices < n-1
-        const int words = max(last, 0) * kRecWords, chunks = words >> 2;
-        for (int c = tid; c < chunks; c += kLeafThreads) {
-            const int r0 = (4 * c) / kRecWords, r1 = (4 * c + 3) / kRecWords;
-            if (own[r0] && own[r1]) {
-                reinterpret_cast<uint4 *>(dst)[c] = reinterpret_cast<const uint4 *>(rec)[c];
-            } else {
-                for (int q = 4 * c; q < 4 * c + 4; ++q)
-                    if (own[q / kRecWords]) dst[q] = rec[q];
-            }
-        }
-        for (int q = 4 * chunks + tid; q < words; q += kLeafThreads)
-            if (own[q / kRecWords]) dst[q] = rec[q];
-    }
-    // ---- climb above the window (thread 0 holds the window's bound)
-    if (tid != 0 || n <= kEmitLeaves) return;
-    climb_blocks(kEmitLog, blockIdx.x, b, n, btn, block_bounds, arrivals, nblocks);
+    if (!s_last) return;
+    __threadfence();
+    if (tid < nsuper)
+        for (int a = 0; a < 6; ++a) b[a] = __ldcg(super_bounds + 6 * (size_t)tid + a);
+    __syncthreads();                                // wb reused
+    reduce_units(b, 0, nsuper, kUpperLog, n, btn, wb);
 }
 
 // the tiles of every segment's tree in one launch
@@ -1455,9 +1582,10 @@ size_t sort_status_words(int n) {
     return tiles * 256 * 5;
 }
 
-// per-level block bounds above the emission windows: 256-leaf windows in the
-// single-tree build (k_emit), 1024-leaf tiles in the batched one -- the
-// former needs more, so both size by it
+// block bounds of the emission: in the single-tree build the 256-leaf
+// windows' bounds, then the climb's levels above 2^16 leaves; in the batched
+// build the levels above the 1024-leaf tiles -- the former needs more, so
+// both size by it
 size_t block_bound_count(int n) {
     const size_t nblocks = ((size_t)n + kEmitLeaves - 1) / kEmitLeaves;
     return 2 * nblocks + 64;
@@ -1543,8 +1671,15 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
                        (const uint32_t *)b.keys_alt, (const int32_t *)b.vals_alt, (uint32_t *)nullptr, b.sorted,
                        n, 3, b.state, b.status + 3 * pass_words, no_seg, 0);
     if (e != cudaSuccess) return e;
-    e = launch_chained(k_emit, nblocks, kLeafThreads, 0, s, (const float4 *)b.aabbs, (const int32_t *)b.sorted,
-                       n, b.btl, b.btn, b.block_bounds, b.arrivals, nblocks);
+    // window bounds first in block_bounds, then the climb's levels from 2^16 up
+    const int nsuper = (nblocks + 255) / 256;
+    e = launch_chained(k_emit, min(nblocks, sm_count * PTGPU_EMIT_MINBLOCKS), kLeafThreads, 0, s,
+                       (const float4 *)b.aabbs, (const int32_t *)b.sorted, n, b.btl, b.btn, b.block_bounds,
+                       nblocks);
+    if (e != cudaSuccess) return e;
+    if (nblocks > 1)
+        e = launch_chained(k_emit_upper, nsuper, 256, 0, s, (const float *)b.block_bounds, nblocks, n, b.btn,
+                           b.block_bounds + 6 * (size_t)nblocks, b.arrivals, nsuper);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }

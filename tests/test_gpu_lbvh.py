@@ -66,13 +66,16 @@ def test_lbvh_1m(n, built_lib, orc):
     _compare(scenes.triangle_soup(n, seed=5), orc)
 
 
-def test_lbvh_4m_properties(built_lib):
-    """4M triangles: size-independent checks -- each shape exactly once in the
-    leaves, keys non-increasing along the leaves, every internal bound equal
-    to the union of its children, parents consistent."""
-    n = 1 << 22
+@pytest.mark.parametrize("n", [1 << 22, (1 << 24) + 7])
+def test_lbvh_large_properties(n, built_lib):
+    """4M and 16.7M triangles (the second climbs above 2^24 leaves with
+    arrival counters): size-independent checks -- each shape exactly once in
+    the leaves, keys non-increasing along the leaves, stable ties, every
+    internal bound equal to the union of its children, the children's ranges
+    splitting the parent's at nLeft, and parents pointing back."""
     shapes = scenes.triangle_soup(n, seed=6)
     g_shapes, btn, btl, ms = _gpu_build(shapes)
+    del shapes
     order = btl["nShape"]
     assert np.array_equal(np.sort(order), np.arange(n))
     keys = g_shapes["morton_code"][order]
@@ -80,6 +83,7 @@ def test_lbvh_4m_properties(built_lib):
     # stability: equal keys keep index order
     eq = keys[:-1] == keys[1:]
     assert (order[:-1][eq] < order[1:][eq]).all()
+    del keys, eq, order, g_shapes
     ll = btn["nLeft"] == btn["min"]
     rl = btn["nRight"] == btn["max"]
     lb = np.where(ll[:, None], btl["bound"][btn["nLeft"]], btn["bound"][np.minimum(btn["nLeft"], n - 2)])
@@ -88,6 +92,22 @@ def test_lbvh_4m_properties(built_lib):
     maxs = np.where(lb[:, 1::2] > rb[:, 1::2], lb[:, 1::2], rb[:, 1::2])
     assert np.array_equal(btn["bound"][:, 0::2], mins)
     assert np.array_equal(btn["bound"][:, 1::2], maxs)
+    del lb, rb, mins, maxs
+    idx = np.arange(n - 1, dtype=np.int32)
+    nl, nr = btn["nLeft"], btn["nRight"]
+    assert np.array_equal(nr, nl + 1)
+    assert btn["min"][0] == 0 and btn["max"][0] == n - 1
+    # internal children: ranges [min, nLeft] and [nRight, max], parent = this node
+    li = ~ll
+    assert np.array_equal(btn["min"][nl[li]], btn["min"][li])
+    assert np.array_equal(btn["max"][nl[li]], nl[li])
+    assert np.array_equal(btn["nParent"][nl[li]], idx[li])
+    ri = ~rl
+    assert np.array_equal(btn["min"][nr[ri]], nr[ri])
+    assert np.array_equal(btn["max"][nr[ri]], btn["max"][ri])
+    assert np.array_equal(btn["nParent"][nr[ri]], idx[ri])
+    assert np.array_equal(btl["nParent"][nl[ll]], idx[ll])
+    assert np.array_equal(btl["nParent"][nr[rl]], idx[rl])
     assert ms > 0
 
 
