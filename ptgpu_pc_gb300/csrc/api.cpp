@@ -93,7 +93,7 @@ struct ptgpu_ctx {
     int accel_built = -1;
     bool bvh_valid = false;
     DevBuf d_btn, d_btl, d_keys, d_keys_alt, d_keys_tmp, d_vals_alt, d_vals_tmp, d_sorted;
-    DevBuf d_status, d_state, d_block_bounds, d_arrivals, d_tcount, d_tcost, d_aabbs, d_lb;
+    DevBuf d_status, d_state, d_block_bounds, d_arrivals, d_tcount, d_tcost, d_aabbs;
     DevBuf d_nodes, d_nodes4, d_prims, d_prim_id, d_root_box, d_identity;
     int n_internal = 0;
     bool wide = false;
@@ -224,7 +224,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
     DevBuf *bufs[] = {&c->d_shapes, &c->d_verts, &c->d_type, &c->d_prims0, &c->d_mats, &c->d_lights,
                       &c->d_btn, &c->d_btl, &c->d_keys, &c->d_keys_alt, &c->d_keys_tmp, &c->d_vals_alt,
                       &c->d_vals_tmp, &c->d_sorted, &c->d_status, &c->d_state, &c->d_block_bounds, &c->d_arrivals,
-                      &c->d_tcount, &c->d_tcost, &c->d_aabbs, &c->d_lb,
+                      &c->d_tcount, &c->d_tcost, &c->d_aabbs,
                       &c->d_nodes, &c->d_nodes4, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_wf, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
@@ -346,7 +346,6 @@ static int ensure_bvh_buffers(ptgpu_ctx *c) {
     CK(c->d_btn.ensure((n > 1 ? n - 1 : 1) * sizeof(ptgpu_bvh_node)));
     CK(c->d_btl.ensure(n * sizeof(ptgpu_bvh_node)));
     CK(c->d_aabbs.ensure(n * 2 * sizeof(float4)));
-    CK(c->d_lb.ensure(n * 2 * sizeof(float4)));
     CK(c->d_keys.ensure(n * 4));
     CK(c->d_keys_alt.ensure(n * 4));
     CK(c->d_keys_tmp.ensure(n * 4));
@@ -407,7 +406,7 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
         b.verts = c->d_verts.as<float>();
         b.type = c->d_type.as<uint8_t>();
         b.aabbs = c->d_aabbs.as<float4>();
-        b.leaf_bounds = c->d_lb.as<float4>();
+        b.leaf_bounds = nullptr;                 // batched builds only
         b.keys = c->d_keys.as<uint32_t>();
         b.keys_alt = c->d_keys_alt.as<uint32_t>();
         b.keys_tmp = c->d_keys_tmp.as<uint32_t>();

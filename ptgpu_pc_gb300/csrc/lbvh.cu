@@ -148,28 +148,31 @@ __global__ void k_init_state(BuildState *st) {
 // Centroid bounds, and each shape's bound stored as one aligned 32-byte
 // record for the later kernels (the emission kernel gathers it in sorted
 // order: one sector per leaf instead of a 36-byte vertex triple).
+// one shape's bound, its 32-byte record and its share of the centroid bounds
+__device__ __forceinline__ void centroid_shape(const float *__restrict__ v, bool tri,
+                                               float4 *__restrict__ rec, float lo[3], float hi[3]) {
+    float b[6];
+    shape_bound(v, 0, tri, b);
+    rec[0] = make_float4(b[0], b[1], b[2], b[3]);
+    rec[1] = make_float4(b[4], b[5], 0.f, 0.f);
+    const float c[3] = {tri ? (b[0] + b[1]) / 2.0f : v[0], tri ? (b[2] + b[3]) / 2.0f : v[1],
+                        tri ? (b[4] + b[5]) / 2.0f : v[2]};
+    for (int a = 0; a < 3; ++a) {
+        if (c[a] == c[a]) {          // NaN centroids never pass the reference's < / >
+            lo[a] = fminf(lo[a], c[a]);
+            hi[a] = fmaxf(hi[a], c[a]);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) k_centroid_bounds(const float *__restrict__ verts,
                                                           const uint8_t *__restrict__ type,
                                                           int all_tri, int n, BuildState *st,
                                                           float4 *__restrict__ aabbs) {
     pdl_begin();
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
-        float b[6];
-        shape_bound(verts, i, tri, b);
-        aabbs[2 * (size_t)i] = make_float4(b[0], b[1], b[2], b[3]);
-        aabbs[2 * (size_t)i + 1] = make_float4(b[4], b[5], 0.f, 0.f);
-        f3 p = tri ? mk3((b[0] + b[1]) / 2.0f, (b[2] + b[3]) / 2.0f, (b[4] + b[5]) / 2.0f)
-                   : shape_centroid(verts, i, false);
-        float c[3] = {p.x, p.y, p.z};
-        for (int a = 0; a < 3; ++a) {
-            if (c[a] == c[a]) {          // NaN centroids never pass the reference's < / >
-                lo[a] = fminf(lo[a], c[a]);
-                hi[a] = fmaxf(hi[a], c[a]);
-            }
-        }
-    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        centroid_shape(verts + 9 * (size_t)i, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i, lo, hi);
     for (int a = 0; a < 3; ++a) {
         for (int o = 16; o > 0; o >>= 1) {
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
@@ -898,6 +901,17 @@ __device__ __forceinline__ void gather_bound(const float4 *__restrict__ aabbs,
     q1 = __ldg(aabbs + 2 * (size_t)sh + 1);
 }
 
+// stages the record of the block at `level` starting at leaf T0 + l0 into
+// its slot (index - T0) of the window, when it is an internal node there
+__device__ __forceinline__ void stage_block(uint32_t *rec, int T0, int l0, int level, int n, const float b[6]) {
+    const int lo = T0 + l0;
+    const int hi = min(T0 + l0 + (1 << level), n) - 1;
+    const TopoBlock bn = topo_block_fast(lo, hi, level, n);
+    const int j = bn.idx - T0;
+    if (bn.idx >= 0 && bn.idx < n - 1 && j >= 0 && j < kEmitLeaves)
+        stage_node(rec + j * kRecWords, lo, hi, 0, bn.leaf, bn.gamma, bn.gamma + 1, bn.parent, b, 0u, 0u);
+}
+
 __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(const float4 *__restrict__ aabbs,
                                                         const int32_t *__restrict__ sorted, int n,
                                                         ptgpu_bvh_node *__restrict__ btl,
@@ -907,7 +921,6 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
     __shared__ __align__(16) uint32_t rec[kEmitLeaves * kRecWords];
     __shared__ float slot_b[8][32 * 7];     // per warp: the bounds of its 31 nodes, 7 floats apart
     __shared__ float wb[8 * 6];
-    __shared__ unsigned char own[kEmitLeaves];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     float *sb = slot_b[w];
     int win = blockIdx.x;
@@ -921,9 +934,8 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
         const int kn = (win + (int)gridDim.x) * kEmitLeaves + tid;
         const bool have_n = win + (int)gridDim.x < nblocks && kn < n;
         float b[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y}, c[6];
-        own[tid] = 0;
         if (have) {
-            const int parent = n >= 2 ? topo_parent_leaf(k0 + tid, n) : -1;
+            const int parent = n >= 2 ? topo_parent_leaf_fast(k0 + tid, n) : -1;
             stage_node(rec + tid * kRecWords, -1, -1, sh, -1, -1, -1, parent, b, 0xffffffffu, 0xffffffffu);
         }
         // ---- levels 1-5 inside the warp; level L parks its bounds in
@@ -961,7 +973,7 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
                 float nb[6];
 #pragma unroll
                 for (int a = 0; a < 6; ++a) nb[a] = sb[lane * 7 + a];
-                block_record<kEmitLeaves>(rec, own, k0, 32 * w + lo_w, level, n, nb);
+                stage_block(rec, k0, 32 * w + lo_w, level, n, nb);
             }
         }
         // ---- levels 6-8 over the 8 warps, in warp 0
@@ -977,30 +989,24 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
                 const bool leader = (lane & ((off << 1) - 1)) == 0;
                 if (leader && h && wl0 + (1 << (level - 1)) < cnt) {
                     merge6(b, c);
-                    block_record<kEmitLeaves>(rec, own, k0, wl0, level, n, b);
+                    stage_block(rec, k0, wl0, level, n, b);
                 }
             }
             if (lane == 0)
                 for (int a = 0; a < 6; ++a) win_bounds[6 * (size_t)win + a] = b[a];
         }
         __syncthreads();
-        {   // 16-byte chunks whose records the window owns; words elsewhere
+        {   // every slot of the window: the one slot (at most) that belongs to a
+            // node above the window gets a stale record here, which
+            // k_emit_upper overwrites after this kernel ends
             uint32_t *dst = reinterpret_cast<uint32_t *>(btn + k0);
             const int last = min(kEmitLeaves, n - 1 - k0);     // internal indices < n-1
             const int words = max(last, 0) * kRecWords, chunks = words >> 2;
-            for (int q = tid; q < chunks; q += kLeafThreads) {
-                const int r0 = (4 * q) / kRecWords, r1 = (4 * q + 3) / kRecWords;
-                if (own[r0] && own[r1]) {
-                    reinterpret_cast<uint4 *>(dst)[q] = reinterpret_cast<const uint4 *>(rec)[q];
-                } else {
-                    for (int x = 4 * q; x < 4 * q + 4; ++x)
-                        if (own[x / kRecWords]) dst[x] = rec[x];
-                }
-            }
-            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads)
-                if (own[q / kRecWords]) dst[q] = rec[q];
+            for (int q = tid; q < chunks; q += kLeafThreads)
+                reinterpret_cast<uint4 *>(dst)[q] = reinterpret_cast<const uint4 *>(rec)[q];
+            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) dst[q] = rec[q];
         }
-        __syncthreads();                            // rec, own and the slots are reused
+        __syncthreads();                            // rec and the slots are reused
     }
 }
 

@@ -26,7 +26,7 @@ struct LbvhBuffers {
     const float *verts;         // 9 floats per shape (p1,p2,p3 or centre,rad)
     const uint8_t *type;        // PTGPU_SPHERE / PTGPU_TRIANGLE per shape
     float4 *aabbs;              // 2 per shape: (min_x,max_x,min_y,max_y), (min_z,max_z,-,-)
-    float4 *leaf_bounds;        // the same records in sorted (leaf) order
+    float4 *leaf_bounds;        // the same records in sorted (leaf) order (batched build)
     uint32_t *keys;             // ~Morton code per shape (sort key)
     uint32_t *keys_alt, *keys_tmp;
     int32_t *vals_alt, *vals_tmp;

@@ -156,4 +156,13 @@ __host__ __device__ __forceinline__ TopoBlock topo_block_fast(int32_t lo, int32_
     return r;
 }
 
+// topo_parent_leaf in a few integer operations: the 2-leaf block [2j, 2j+1]
+// (j = k / 2) is numbered by its end when it is a left child and by its
+// start when a right child, whenever the block and its sibling exist.
+__host__ __device__ __forceinline__ int32_t topo_parent_leaf_fast(int32_t k, int32_t n) {
+    const int32_t j = k >> 1;
+    if (2 * (int64_t)(j + 1) <= n && 2 * (int64_t)(j ^ 1) < n) return (j & 1) ? 2 * j : 2 * j + 1;
+    return topo_parent_leaf(k, n);
+}
+
 }  // namespace ptgpu

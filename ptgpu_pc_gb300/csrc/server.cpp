@@ -172,7 +172,7 @@ struct ptgpu_server {
     Arena nodes, prims, prim_id, mats, prims0, lights, colors, pixels, seeds;
     DevBuf d_recs, d_pix_start, d_pixctr, d_err, d_seg, d_depth;
     // single-scene build scratch
-    DevBuf s_shapes, s_verts, s_type, s_aabbs, s_lb, s_keys, s_keys_alt, s_keys_tmp, s_vals_alt,
+    DevBuf s_shapes, s_verts, s_type, s_aabbs, s_keys, s_keys_alt, s_keys_tmp, s_vals_alt,
         s_vals_tmp, s_sorted, s_status, s_state, s_bb, s_arr, s_btn, s_btl, s_tcount, s_tcost;
     std::atomic<int> n_active{0};                                 // active.size() for readers
     // counters (guarded by mu)
@@ -294,7 +294,6 @@ int build_scene(ptgpu_server *s, int id) {
     SK(s->s_verts.ensure(N * 9 * sizeof(float)));
     SK(s->s_type.ensure(N));
     SK(s->s_aabbs.ensure(N * 2 * sizeof(float4)));
-    SK(s->s_lb.ensure(N * 2 * sizeof(float4)));
     SK(s->s_keys.ensure(N * 4));
     SK(s->s_keys_alt.ensure(N * 4));
     SK(s->s_keys_tmp.ensure(N * 4));
@@ -317,7 +316,7 @@ int build_scene(ptgpu_server *s, int id) {
     b.verts = s->s_verts.as<float>();
     b.type = s->s_type.as<uint8_t>();
     b.aabbs = s->s_aabbs.as<float4>();
-    b.leaf_bounds = s->s_lb.as<float4>();
+    b.leaf_bounds = nullptr;                     // batched builds only
     b.keys = s->s_keys.as<uint32_t>();
     b.keys_alt = s->s_keys_alt.as<uint32_t>();
     b.keys_tmp = s->s_keys_tmp.as<uint32_t>();
@@ -616,7 +615,7 @@ int ptgpu_server_destroy(ptgpu_server *s) {
                    &s->colors, &s->pixels, &s->seeds};
     for (Arena *a : as) a->buf.release();
     DevBuf *bufs[] = {&s->d_recs, &s->d_pix_start, &s->d_pixctr, &s->d_err, &s->d_seg, &s->d_depth,
-                      &s->s_shapes, &s->s_verts, &s->s_lb,
+                      &s->s_shapes, &s->s_verts,
                       &s->s_type, &s->s_aabbs, &s->s_keys, &s->s_keys_alt, &s->s_keys_tmp,
                       &s->s_vals_alt, &s->s_vals_tmp, &s->s_sorted, &s->s_status, &s->s_state,
                       &s->s_bb, &s->s_arr, &s->s_btn, &s->s_btl, &s->s_tcount, &s->s_tcost};

@@ -27,7 +27,8 @@ void shim_topology(int n, int *mn, int *mx, int *gamma, int *parent, int *leaf, 
 
 // Every block of 2^L leaves with both halves non-empty: the short form of its
 // record fields against the general one, and the general one against the
-// node that carries its index.  Returns the number of mismatches.
+// node that carries its index; every leaf's parent in short and general
+// form.  Returns the number of mismatches.
 int shim_check_blocks(int n) {
     int bad = 0;
     for (int level = 1; level < 31 && (1 << (level - 1)) < n; ++level) {
@@ -42,6 +43,8 @@ int shim_check_blocks(int n) {
             if (t.lo != (int)lo || t.hi != hi || t.gamma != g.gamma || t.parent != g.parent || leaf != g.leaf) ++bad;
         }
     }
+    for (int k = 0; k < n; ++k)
+        if (ptgpu::topo_parent_leaf_fast(k, n) != ptgpu::topo_parent_leaf(k, n)) ++bad;
     return bad;
 }
 
