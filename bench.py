@@ -45,6 +45,7 @@ SPP = 16
 MAX_DEPTH = 8
 LBVH_N = 1 << 22
 RAYS_N = 1 << 24
+INGEST_N = 1_000_000
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = "icosphere_81934tri_512x512_16spp_depth8_bvh"
 TREELET_ROUNDS = 2
@@ -265,6 +266,37 @@ def bench_closest(ctx, torch, scenes, warmup, steps):
     m = float(np.mean(ms))
     return {"metric": "closest-hit Mrays/s", "rays": RAYS_N, "n_tris": LBVH_N,
             "value": RAYS_N / m / 1e3, "unit": "Mrays/s", "ms": m, "hit_fraction": hits / RAYS_N}
+
+
+def bench_ingest(pt, abi, scenes, n_tris=INGEST_N, reps=3):
+    """Scene-file ingestion: a seeded .txt scene with two OBJ models (n_tris
+    triangles, ~38 MB of text at 1M) loaded by ptgpu_read_scene (models
+    expanded into shapes on the host, then copied) and by ptgpu_stream_scene
+    (vertex and index arrays copied, shapes expanded on the device).  Both
+    read the OBJ files on the host threads; wall time of the call, best of
+    reps, in a fresh context each time."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = scenes.write_model_scene(d, n_tris, seed=11)
+        size = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+        best = {}
+        n = 0
+        for mode in ("read", "stream"):
+            for _ in range(reps):
+                ctx = pt.Context(8, 8)
+                t0 = time.perf_counter()
+                if mode == "read":
+                    ctx.read_scene(path)
+                else:
+                    ctx.stream_scene(path)
+                dt = time.perf_counter() - t0
+                n = ctx.n
+                ctx.close()
+                best[mode] = min(best.get(mode, 1e30), dt)
+    return {"metric": "scene ingestion Mshapes/s", "shapes": n, "file_bytes": size,
+            "value": n / best["stream"] / 1e6, "unit": "Mshapes/s", "ms": best["stream"] * 1e3,
+            "read_scene_value": n / best["read"] / 1e6, "read_scene_ms": best["read"] * 1e3,
+            "host_threads": os.cpu_count()}
 
 
 def served_requests(specs, n_req, rate, seed=5, hit=0.7):
@@ -543,6 +575,7 @@ def main():
         line["lbvh"] = lb
         line["closest_hit"] = bench_closest(lctx, torch, scenes, 1, 3)
         lctx.close()
+        line["ingest"] = bench_ingest(pt, abi, scenes)
         if not args.no_batched:
             data, specs, line["batched"] = bench_batched(pt, abi, scenes, torch)
             line["served"] = bench_served(pt, abi, data, specs)

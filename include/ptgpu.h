@@ -139,6 +139,14 @@ int  ptgpu_abi_version(void);
  * smallptGPU.cpp:1448-1459): ".txt", ".scn" dispatch by extension.  Sets the
  * context's shapes, light count and camera (orig/target, pitch=yaw=0).        */
 int  ptgpu_read_scene(ptgpu_ctx *ctx, const char *path, int32_t *walllight);
+/* The same scene as ptgpu_read_scene (same shapes byte for byte, light count,
+ * camera, walllight) without a host copy of the shape array: OBJ models are
+ * read on several host threads into vertex and index arrays, copied as they
+ * are, and expanded into Shape records on the device (ReadTxt's model
+ * branch, displayfunc.cpp:395-420, done on the GPU).  Calls that need the
+ * shapes on the host later (ptgpu_get_shapes before a BVH build, the host KD
+ * build) copy them back once. */
+int  ptgpu_stream_scene(ptgpu_ctx *ctx, const char *path, int32_t *walllight);
 /* Copies n shapes in (the global `shapes`/`shapeCnt`/`lightCnt`). */
 int  ptgpu_set_shapes(ptgpu_ctx *ctx, const ptgpu_shape *shapes, uint32_t n,
                       uint32_t light_cnt);
@@ -302,6 +310,15 @@ int  ptgpu_server_destroy(ptgpu_server *s);    /* finishes admitted work first *
 /* Registers a scene (copied); built on its first request with build_flags. */
 int  ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t n,
                             uint32_t light_cnt, uint32_t build_flags, int32_t *scene);
+/* A scene by its file (ptgpu_read_scene's formats, wall light included when
+ * the file asks for it): read once here to check it and count its shapes,
+ * then read again -- models expanded on the device, as ptgpu_stream_scene
+ * does -- every time it has to be built (first use, or after eviction); no
+ * host copy of its shapes is kept.  The file's camera is not used (requests
+ * carry theirs).  Requests on it render as on ptgpu_server_add_scene with
+ * ptgpu_read_scene's shapes. */
+int  ptgpu_server_add_scene_file(ptgpu_server *s, const char *path, uint32_t build_flags,
+                                 int32_t *scene);
 int  ptgpu_server_submit(ptgpu_server *s, const ptgpu_request *r, int64_t *ticket);
 /* Blocks until the request is done, copies its W*H pixels and colours (either
  * may be NULL) and its stats, and forgets the ticket.  PTGPU_E_RANGE: the

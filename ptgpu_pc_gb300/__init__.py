@@ -18,7 +18,7 @@ LIB_PATH = os.environ.get("PTGPU_LIB", os.path.join(HERE, "libptgpu.so"))
 # every entry point declared in include/ptgpu.h
 EXPORTS = [
     "ptgpu_create", "ptgpu_destroy", "ptgpu_status_string", "ptgpu_last_error",
-    "ptgpu_abi_version", "ptgpu_read_scene", "ptgpu_set_shapes", "ptgpu_get_shape_count",
+    "ptgpu_abi_version", "ptgpu_read_scene", "ptgpu_stream_scene", "ptgpu_set_shapes", "ptgpu_get_shape_count",
     "ptgpu_get_shapes", "ptgpu_update_camera", "ptgpu_set_camera", "ptgpu_get_camera",
     "ptgpu_build", "ptgpu_get_bvh", "ptgpu_get_kdtree", "ptgpu_set_bvh", "ptgpu_last_build_ms",
     "ptgpu_make_seeds", "ptgpu_set_seeds", "ptgpu_get_seeds", "ptgpu_reset_accumulation",
@@ -29,7 +29,8 @@ EXPORTS = [
     "ptgpu_batch_create", "ptgpu_batch_destroy", "ptgpu_batch_add", "ptgpu_batch_build",
     "ptgpu_batch_tune", "ptgpu_batch_render", "ptgpu_batch_reset", "ptgpu_batch_get_pixels",
     "ptgpu_batch_get_colors", "ptgpu_batch_get_bvh", "ptgpu_batch_info_get",
-    "ptgpu_server_create", "ptgpu_server_destroy", "ptgpu_server_add_scene", "ptgpu_server_submit",
+    "ptgpu_server_create", "ptgpu_server_destroy", "ptgpu_server_add_scene", "ptgpu_server_add_scene_file",
+    "ptgpu_server_submit",
     "ptgpu_server_wait", "ptgpu_server_info_get",
 ]
 
@@ -62,6 +63,7 @@ def lib():
         L.ptgpu_create.argtypes = [vp, ctypes.POINTER(vp)]
         L.ptgpu_destroy.argtypes = [vp]
         L.ptgpu_read_scene.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(i32)]
+        L.ptgpu_stream_scene.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(i32)]
         L.ptgpu_set_shapes.argtypes = [vp, vp, u32, u32]
         L.ptgpu_get_shape_count.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
         L.ptgpu_get_shapes.argtypes = [vp, vp, u32]
@@ -84,6 +86,7 @@ def lib():
         L.ptgpu_server_create.argtypes = [i32, ctypes.c_int64, i32, u32, ctypes.POINTER(vp)]
         L.ptgpu_server_destroy.argtypes = [vp]
         L.ptgpu_server_add_scene.argtypes = [vp, vp, u32, u32, u32, ctypes.POINTER(i32)]
+        L.ptgpu_server_add_scene_file.argtypes = [vp, ctypes.c_char_p, u32, ctypes.POINTER(i32)]
         L.ptgpu_server_submit.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_int64)]
         L.ptgpu_server_wait.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
         L.ptgpu_server_info_get.argtypes = [vp, vp]
@@ -169,6 +172,16 @@ class Context:
     def read_scene(self, path):
         wl = ctypes.c_int32()
         _check(lib().ptgpu_read_scene(self._h, path.encode(), ctypes.byref(wl)))
+        n, lc = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(lib().ptgpu_get_shape_count(self._h, ctypes.byref(n), ctypes.byref(lc)))
+        self.n = n.value
+        return wl.value
+
+    def stream_scene(self, path):
+        """read_scene without a host copy of the shapes: models are read on
+        host threads and expanded into shapes on the device."""
+        wl = ctypes.c_int32()
+        _check(lib().ptgpu_stream_scene(self._h, path.encode(), ctypes.byref(wl)))
         n, lc = ctypes.c_uint32(), ctypes.c_uint32()
         _check(lib().ptgpu_get_shape_count(self._h, ctypes.byref(n), ctypes.byref(lc)))
         self.n = n.value
@@ -395,6 +408,13 @@ class Server:
         sid = ctypes.c_int32()
         _check(lib().ptgpu_server_add_scene(self._h, shapes.ctypes.data, len(shapes), light_cnt,
                                             build_flags, ctypes.byref(sid)))
+        return sid.value
+
+    def add_scene_file(self, path, build_flags=0):
+        """A scene by its file, read again (models expanded on the device)
+        whenever it has to be built."""
+        sid = ctypes.c_int32()
+        _check(lib().ptgpu_server_add_scene_file(self._h, path.encode(), build_flags, ctypes.byref(sid)))
         return sid.value
 
     def submit(self, scene, camera, width, height, spp, seed, max_depth=0):

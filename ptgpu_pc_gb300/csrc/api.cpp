@@ -14,6 +14,7 @@
 
 #include "devbuf.h"
 #include "host.h"
+#include "ingest.h"
 #include "lbvh.h"
 
 using namespace ptgpu;
@@ -83,7 +84,10 @@ struct ptgpu_ctx {
     int block = 128;
     int flags = 0;
     // scene
-    std::vector<ptgpu_shape> h_shapes;
+    std::vector<ptgpu_shape> h_shapes;   // empty after ptgpu_stream_scene (device copy only)
+    bool host_shapes = false;            // h_shapes holds the scene
+    bool kd_indexed = false;             // a KD build numbered the host copy's shapes
+    IngestScratch ingest;
     uint32_t n = 0, light_cnt = 0;
     int n_lights = 0;
     bool all_tri = true;
@@ -229,6 +233,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_wf, &c->d_rays, &c->d_t,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
+    c->ingest.release();
     kd_scratch_destroy(c->kd_scratch);
     if (c->h_pixels) cudaFreeHost(c->h_pixels);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -244,6 +249,41 @@ int ptgpu_get_stream(ptgpu_ctx *c, void **stream) {
     return PTGPU_OK;
 }
 
+// Device arrays of a scene of n shapes with n_lights light records.
+static int alloc_scene(ptgpu_ctx *c, uint32_t n, int n_lights) {
+    CK(c->d_shapes.ensure((size_t)n * sizeof(ptgpu_shape)));
+    CK(c->d_verts.ensure((size_t)n * 9 * sizeof(float)));
+    CK(c->d_type.ensure((size_t)n));
+    CK(c->d_prims0.ensure((size_t)n * 3 * sizeof(float4)));
+    CK(c->d_mats.ensure((size_t)n * sizeof(Material)));
+    CK(c->d_lights.ensure((size_t)n_lights * sizeof(LightRec)));
+    CK(c->d_identity.ensure((size_t)n * sizeof(int32_t)));
+    return PTGPU_OK;
+}
+
+// The rest of a scene upload once d_shapes and d_lights hold it: the build
+// and traversal arrays derived from the shapes, and a fresh accumulation.
+static int finish_scene(ptgpu_ctx *c, uint32_t n, uint32_t light_cnt, int n_lights, bool all_tri) {
+    c->n = n;
+    c->light_cnt = light_cnt;
+    c->n_lights = n_lights;
+    c->all_tri = all_tri;
+    std::vector<int32_t> ident(n);
+    for (uint32_t i = 0; i < n; ++i) ident[i] = (int32_t)i;
+    CK(cudaMemcpyAsync(c->d_identity.p, ident.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_unpack_shapes(c->d_shapes.as<ptgpu_shape>(), (int)n, c->d_verts.as<float>(),
+                            c->d_type.as<uint8_t>(), c->d_prims0.as<float4>(), c->d_mats.as<Material>(),
+                            c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->accel_built = -1;
+    c->bvh_valid = false;
+    c->kd_valid = false;
+    c->shapes_exported = false;
+    c->kd_indexed = false;
+    c->current_sample = 0;
+    return PTGPU_OK;
+}
+
 int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt) {
     if (!c || (!shapes && n)) return fail(PTGPU_E_INVAL, "null argument");
     if (n == 0) return fail(PTGPU_E_INVAL, "a scene needs at least one shape");
@@ -253,36 +293,37 @@ int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32
             return fail(PTGPU_E_INVAL, "shape " + std::to_string(i) + " has an unknown type");
     cudaSetDevice(c->device);
     c->h_shapes.assign(shapes, shapes + n);
-    c->n = n;
-    c->light_cnt = light_cnt;
-    c->all_tri = true;
-    for (uint32_t i = 0; i < n; ++i) if (shapes[i].type != PTGPU_TRIANGLE) { c->all_tri = false; break; }
+    c->host_shapes = true;
+    bool all_tri = true;
+    for (uint32_t i = 0; i < n; ++i) if (shapes[i].type != PTGPU_TRIANGLE) { all_tri = false; break; }
     // emitters visited by SampleLights: the first light_cnt in index order
     std::vector<LightRec> lights;
     make_lights(shapes, n, light_cnt, lights);
-    c->n_lights = (int)lights.size();
-    CK(c->d_shapes.ensure((size_t)n * sizeof(ptgpu_shape)));
-    CK(c->d_verts.ensure((size_t)n * 9 * sizeof(float)));
-    CK(c->d_type.ensure((size_t)n));
-    CK(c->d_prims0.ensure((size_t)n * 3 * sizeof(float4)));
-    CK(c->d_mats.ensure((size_t)n * sizeof(Material)));
-    CK(c->d_lights.ensure(lights.size() * sizeof(LightRec)));
-    CK(c->d_identity.ensure((size_t)n * sizeof(int32_t)));
-    std::vector<int32_t> ident(n);
-    for (uint32_t i = 0; i < n; ++i) ident[i] = (int32_t)i;
+    int st = alloc_scene(c, n, (int)lights.size());
+    if (st) return st;
     CK(cudaMemcpyAsync(c->d_shapes.p, shapes, (size_t)n * sizeof(ptgpu_shape), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_identity.p, ident.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
     if (!lights.empty())
         CK(cudaMemcpyAsync(c->d_lights.p, lights.data(), lights.size() * sizeof(LightRec), cudaMemcpyHostToDevice, c->stream));
-    CK(launch_unpack_shapes(c->d_shapes.as<ptgpu_shape>(), (int)n, c->d_verts.as<float>(),
-                            c->d_type.as<uint8_t>(), c->d_prims0.as<float4>(), c->d_mats.as<Material>(),
-                            c->stream));
+    return finish_scene(c, n, light_cnt, (int)lights.size(), all_tri);
+}
+
+// The host copy of the scene, for the calls that need one after
+// ptgpu_stream_scene: the device records with the fields a BVH build exports
+// (index, morton_code, b) as the host copy would hold them -- the loader's
+// zeros, or the index a KD build gives.
+static int ensure_host_shapes(ptgpu_ctx *c) {
+    if (c->host_shapes) return PTGPU_OK;
+    c->h_shapes.resize(c->n);
+    CK(cudaMemcpyAsync(c->h_shapes.data(), c->d_shapes.p, (size_t)c->n * sizeof(ptgpu_shape),
+                       cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    c->accel_built = -1;
-    c->bvh_valid = false;
-    c->kd_valid = false;
-    c->shapes_exported = false;
-    c->current_sample = 0;
+    for (uint32_t i = 0; i < c->n; ++i) {
+        ptgpu_shape &s = c->h_shapes[i];
+        s.index = c->kd_indexed ? (int32_t)i : 0;
+        s.morton_code = 0;
+        std::memset(&s.b, 0, sizeof(s.b));
+    }
+    c->host_shapes = true;
     return PTGPU_OK;
 }
 
@@ -307,6 +348,8 @@ int ptgpu_get_shapes(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
         CK(cudaStreamSynchronize(c->stream));
         return PTGPU_OK;
     }
+    int st = ensure_host_shapes(c);
+    if (st) return st;
     std::memcpy(out, c->h_shapes.data(), (size_t)n * sizeof(ptgpu_shape));
     return PTGPU_OK;
 }
@@ -320,6 +363,30 @@ int ptgpu_read_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
     if (sc.walllight) add_wall_light(sc);      // main(): if (walllight) AddWallLight()
     if (walllight) *walllight = sc.walllight ? 1 : 0;
     st = ptgpu_set_shapes(c, sc.shapes.data(), (uint32_t)sc.shapes.size(), sc.light_cnt);
+    if (st != PTGPU_OK) return st;
+    return ptgpu_set_camera(c, &sc.camera);
+}
+
+int ptgpu_stream_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
+    if (!c || !path) return fail(PTGPU_E_INVAL, "null argument");
+    CompactScene sc;
+    std::string err;
+    int st = read_scene_compact(path, c->w, c->h, sc, err);
+    if (st != PTGPU_OK) return fail(st, err);
+    if (sc.walllight) add_wall_light(sc);      // main(): if (walllight) AddWallLight()
+    if (walllight) *walllight = sc.walllight ? 1 : 0;
+    const int64_t n = sc.count();
+    if (n == 0) return fail(PTGPU_E_INVAL, "a scene needs at least one shape");
+    if (n >= (1 << 30)) return fail(PTGPU_E_INVAL, "too many shapes (limit 2^30-1)");
+    cudaSetDevice(c->device);
+    const uint32_t n_lights = compact_light_count(sc);
+    st = alloc_scene(c, (uint32_t)n, (int)n_lights);
+    if (st) return st;
+    c->h_shapes.clear();
+    c->h_shapes.shrink_to_fit();
+    c->host_shapes = false;
+    CK(ingest_compact(sc, c->d_shapes.as<ptgpu_shape>(), c->d_lights.as<LightRec>(), c->ingest, c->stream));
+    st = finish_scene(c, (uint32_t)n, sc.light_cnt, (int)n_lights, compact_all_triangles(sc));
     if (st != PTGPU_OK) return st;
     return ptgpu_set_camera(c, &sc.camera);
 }
@@ -446,7 +513,9 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
     // host build), device traversal
     auto t0 = std::chrono::steady_clock::now();
     if (flags & PTGPU_FLAG_KD_HOST) {
-        int st = kd_build(c->h_shapes.data(), c->n, c->kd);
+        int st = ensure_host_shapes(c);
+        if (st) return st;
+        st = kd_build(c->h_shapes.data(), c->n, c->kd);
         if (st) return fail(st, "kd build failed");
     } else {
         if (!c->kd_scratch) c->kd_scratch = kd_scratch_create();
@@ -454,7 +523,9 @@ int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
                         c->stream));
     }
     int st;
-    for (uint32_t i = 0; i < c->n; ++i) { c->h_shapes[i].index = (int32_t)i; c->h_shapes[i].morton_code = 0; }
+    if (c->host_shapes)
+        for (uint32_t i = 0; i < c->n; ++i) { c->h_shapes[i].index = (int32_t)i; c->h_shapes[i].morton_code = 0; }
+    c->kd_indexed = true;
     std::vector<float> nodes;
     float root_box[6];
     kd_trace_nodes(c->kd, nodes, &c->root_first, &c->root_count, root_box);

@@ -43,6 +43,43 @@ struct LoadedScene {
 int read_scene(const char *path, int width, int height, LoadedScene &out, std::string &err);
 void add_wall_light(LoadedScene &sc);      // AddWallLight (smallptGPU.cpp:1448-1459)
 
+// OBJ model as read: x,y,z per vertex, 3 vertex indices per triangle (faces
+// with more than three vertices fanned).  threads <= 0: one host thread per
+// MiB of file, at most 16.
+struct Obj {
+    std::vector<float> v;
+    std::vector<int32_t> tri;
+};
+bool read_obj(const char *path, Obj &obj, std::string &err, int threads = 0);
+
+// The same scene without its model triangles expanded: segments in file
+// order, each either shapes as read_scene gives them or one model kept as
+// vertices + triangle indices with its placement and material.  Expanding
+// every segment in order gives read_scene's shapes.
+struct SceneSegment {
+    bool model = false;
+    std::vector<ptgpu_shape> shapes;             // !model
+    Obj obj;                                     // model
+    ptgpu_vec pos{}, scale{}, e{}, c{};
+    int32_t refl = 0;
+    int64_t count() const { return model ? (int64_t)(obj.tri.size() / 3) : (int64_t)shapes.size(); }
+};
+struct CompactScene {
+    std::vector<SceneSegment> segs;
+    uint32_t light_cnt = 0;
+    ptgpu_camera camera{};
+    bool walllight = true;
+    int64_t count() const {
+        int64_t n = 0;
+        for (const SceneSegment &g : segs) n += g.count();
+        return n;
+    }
+};
+int read_scene_compact(const char *path, int width, int height, CompactScene &out, std::string &err);
+void add_wall_light(CompactScene &sc);
+// a model triangle as read_scene expands it (scaled, translated, area)
+ptgpu_shape model_shape(const SceneSegment &g, size_t t);
+
 // ---- camera / seeds -------------------------------------------------------------
 void update_camera(ptgpu_camera *cam);     // UpdateCamera (displayfunc.cpp:732-756)
 void make_seeds(uint64_t master, uint32_t *seeds, uint32_t count);

@@ -19,6 +19,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "host.h"
@@ -48,11 +50,6 @@ float triangle_area(const ptgpu_vec &p1, const ptgpu_vec &p2, const ptgpu_vec &p
     return sqrtf(n.x * n.x + n.y * n.y + n.z * n.z) * 0.5f;
 }
 
-struct Obj {
-    std::vector<float> v;          // x,y,z per vertex
-    std::vector<int32_t> tri;      // 3 vertex indices per triangle
-};
-
 // parses one face vertex token "i", "i/j", "i//k" or "i/j/k" -> 0-based index
 bool face_index(const char *tok, int32_t nverts, int32_t *out) {
     char *end = nullptr;
@@ -65,54 +62,159 @@ bool face_index(const char *tok, int32_t nverts, int32_t *out) {
     return true;
 }
 
-// Splits the file into lines the way the reference's OBJ reader does: the
+// Kind of one OBJ line (a NUL-terminated copy, so that sscanf and strtok_r
+// see exactly the line): 0 other, 1 vertex, 2 face.
+int obj_line_kind(const char *p) {
+    while (*p == ' ' || *p == '\t') ++p;
+    if (p[0] == 'v' && (p[1] == ' ' || p[1] == '\t')) return 1;
+    if (p[0] == 'f' && (p[1] == ' ' || p[1] == '\t')) return 2;
+    return 0;
+}
+
+// The file is split into lines the way the reference's OBJ reader does: the
 // buffer's last byte is taken for a terminator, so only lines ended by '\n',
 // '\0' or a lone '\r' before the final byte count (a file whose last line is
 // followed by a single newline loses that line, as in the reference scenes).
-bool read_obj(const char *path, Obj &obj, std::string &err) {
+inline bool obj_term(const std::string &buf, size_t i, size_t end_idx) {
+    const char ch = buf[i];
+    return ch == '\0' || ch == '\n' || (ch == '\r' && i + 1 < end_idx && buf[i + 1] != '\n');
+}
+
+// A run of whole lines [begin, end) of the file (end is just past a
+// terminator, or the file's end index for the last run).
+struct ObjRun {
+    size_t begin = 0, end = 0;
+    int64_t nv = 0, ntri = 0;        // vertex lines; triangles after fanning
+    int64_t v0 = 0, t0 = 0;          // vertices and triangles before the run
+    bool ok = true;
+    int bad_kind = 0;                // the first malformed line: 1 vertex, 2 face
+};
+
+// Counts vertex lines and fanned triangles of a run.
+void obj_count(const std::string &buf, size_t end_idx, ObjRun &r) {
+    size_t prev = r.begin;
+    for (size_t i = r.begin; i < r.end && i < end_idx; ++i) {
+        if (!obj_term(buf, i, end_idx)) continue;
+        const char *p = buf.data() + prev;
+        const char *q = buf.data() + i;
+        prev = i + 1;
+        while (p < q && (*p == ' ' || *p == '\t')) ++p;
+        if (q - p < 2 || (p[1] != ' ' && p[1] != '\t')) continue;
+        if (p[0] == 'v') {
+            ++r.nv;
+        } else if (p[0] == 'f') {
+            int64_t tok = 0;
+            bool in = false;
+            for (const char *c = p + 2; c < q; ++c) {
+                const bool sep = *c == ' ' || *c == '\t' || *c == '\r' || *c == '\n' || *c == '\0';
+                if (!sep && !in) ++tok;
+                in = !sep;
+                if (*c == '\0') break;          // strtok_r stops at the copy's end
+            }
+            if (tok > 2) r.ntri += tok - 2;
+        }
+    }
+}
+
+// Parses a run into obj.v / obj.tri at the run's vertex and triangle bases.
+void obj_parse(const std::string &buf, size_t end_idx, ObjRun &r, Obj &obj) {
+    std::string line;
+    std::vector<int32_t> face;
+    int64_t nv = r.v0, nt = r.t0;
+    size_t prev = r.begin;
+    for (size_t i = r.begin; i < r.end && i < end_idx; ++i) {
+        if (!obj_term(buf, i, end_idx)) continue;
+        line.assign(buf, prev, i - prev);
+        prev = i + 1;
+        const int kind = obj_line_kind(line.c_str());
+        if (kind == 0) continue;
+        const char *p = line.c_str();
+        while (*p == ' ' || *p == '\t') ++p;
+        if (kind == 1) {
+            float x, y, z;
+            if (std::sscanf(p + 2, "%f %f %f", &x, &y, &z) != 3) { r.ok = false; r.bad_kind = 1; return; }
+            obj.v[3 * nv] = x; obj.v[3 * nv + 1] = y; obj.v[3 * nv + 2] = z;
+            ++nv;
+        } else {
+            face.clear();
+            std::string rest(p + 2);
+            char *save = nullptr;
+            for (char *tok = strtok_r(&rest[0], " \t\r\n", &save); tok; tok = strtok_r(nullptr, " \t\r\n", &save)) {
+                int32_t idx;
+                if (!face_index(tok, (int32_t)nv, &idx)) { r.ok = false; r.bad_kind = 2; return; }
+                face.push_back(idx);
+            }
+            for (size_t k = 2; k < face.size(); ++k) {
+                obj.tri[3 * nt] = face[0]; obj.tri[3 * nt + 1] = face[k - 1]; obj.tri[3 * nt + 2] = face[k];
+                ++nt;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+// The whole file is read once; runs of lines are then counted and parsed on
+// up to `threads` host threads (one run per thread, cut at line ends), each
+// run writing its vertices and triangles at bases known from the counts, so
+// the result is the sequential reader's: same vertices, same triangles in
+// file order, same errors (a face may only use vertices defined above it).
+bool read_obj(const char *path, Obj &obj, std::string &err, int threads) {
     FILE *f = std::fopen(path, "rb");
     if (!f) { err = std::string("cannot open model ") + path; return false; }
     std::string buf;
+    if (std::fseek(f, 0, SEEK_END) == 0) {
+        const long sz = std::ftell(f);
+        if (sz > 0) buf.reserve((size_t)sz);
+        std::fseek(f, 0, SEEK_SET);
+    }
     char chunk[1 << 16];
     size_t got;
     while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.append(chunk, got);
     std::fclose(f);
     if (buf.empty()) { err = "empty model " + std::string(path); return false; }
     const size_t end_idx = buf.size() - 1;
-    std::vector<int32_t> face;
-    size_t prev = 0;
-    for (size_t i = 0; i < end_idx; ++i) {
-        const char ch = buf[i];
-        const bool ending = ch == '\0' || ch == '\n' || (ch == '\r' && i + 1 < end_idx && buf[i + 1] != '\n');
-        if (!ending) continue;
-        std::string line = buf.substr(prev, i - prev);
-        prev = i + 1;
-        const char *p = line.c_str();
-        while (*p == ' ' || *p == '\t') ++p;
-        if (p[0] == 'v' && (p[1] == ' ' || p[1] == '\t')) {
-            float x, y, z;
-            if (std::sscanf(p + 2, "%f %f %f", &x, &y, &z) != 3) {
-                err = "malformed vertex in " + std::string(path); return false;
-            }
-            obj.v.push_back(x); obj.v.push_back(y); obj.v.push_back(z);
-        } else if (p[0] == 'f' && (p[1] == ' ' || p[1] == '\t')) {
-            face.clear();
-            std::string rest(p + 2);
-            char *save = nullptr;
-            for (char *tok = strtok_r(&rest[0], " \t\r\n", &save); tok; tok = strtok_r(nullptr, " \t\r\n", &save)) {
-                int32_t idx;
-                if (!face_index(tok, (int32_t)(obj.v.size() / 3), &idx)) {
-                    err = "malformed face in " + std::string(path); return false;
-                }
-                face.push_back(idx);
-            }
-            for (size_t k = 2; k < face.size(); ++k) {
-                obj.tri.push_back(face[0]); obj.tri.push_back(face[k - 1]); obj.tri.push_back(face[k]);
-            }
+    if (threads <= 0) {
+        const unsigned hw = std::thread::hardware_concurrency();
+        threads = (int)std::min<size_t>(std::max(1u, std::min(hw, 16u)), std::max<size_t>(1, buf.size() >> 20));
+    }
+    // runs cut just past a terminator
+    std::vector<ObjRun> runs;
+    size_t start = 0;
+    for (int t = 0; t < threads && start < end_idx; ++t) {
+        size_t stop = end_idx;
+        if (t + 1 < threads) {
+            size_t i = std::max(start, (size_t)((double)end_idx * (t + 1) / threads));
+            while (i < end_idx && !obj_term(buf, i, end_idx)) ++i;
+            stop = i < end_idx ? i + 1 : end_idx;
         }
+        ObjRun r;
+        r.begin = start;
+        r.end = stop;
+        runs.push_back(r);
+        start = stop;
+    }
+    auto for_runs = [&](auto fn) {
+        std::vector<std::thread> th;
+        for (size_t k = 1; k < runs.size(); ++k) th.emplace_back([&, k] { fn(runs[k]); });
+        if (!runs.empty()) fn(runs[0]);
+        for (auto &x : th) x.join();
+    };
+    for_runs([&](ObjRun &r) { obj_count(buf, end_idx, r); });
+    int64_t nv = 0, nt = 0;
+    for (ObjRun &r : runs) { r.v0 = nv; r.t0 = nt; nv += r.nv; nt += r.ntri; }
+    obj.v.assign((size_t)(3 * nv), 0.f);
+    obj.tri.assign((size_t)(3 * nt), 0);
+    for_runs([&](ObjRun &r) { obj_parse(buf, end_idx, r, obj); });
+    for (const ObjRun &r : runs) {       // the first malformed line in file order
+        if (r.ok) continue;
+        err = (r.bad_kind == 1 ? "malformed vertex in " : "malformed face in ") + std::string(path);
+        return false;
     }
     return true;
 }
+
+namespace {
 
 ptgpu_shape sphere_shape(float rad, ptgpu_vec c, ptgpu_vec e, ptgpu_vec col, int refl) {
     ptgpu_shape s;
@@ -131,13 +233,40 @@ std::string dir_of(const char *path) {
     return slash ? std::string(path, slash - path + 1) : std::string();
 }
 
-int read_txt(const char *path, int width, int height, LoadedScene &sc, std::string &err) {
+// Receives the objects of a .txt scene in file order.
+struct TxtSink {
+    virtual ~TxtSink() = default;
+    virtual void shape(const ptgpu_shape &s) = 0;
+    virtual void model(Obj &&obj, ptgpu_vec pos, ptgpu_vec scale, ptgpu_vec e, ptgpu_vec col, int refl) = 0;
+};
+
+// model triangles as shapes (displayfunc.cpp:395-420): scale then translate
+ptgpu_shape model_triangle(const Obj &obj, size_t t, ptgpu_vec pos, ptgpu_vec scale, ptgpu_vec e,
+                           ptgpu_vec col, int refl) {
+    ptgpu_shape s;
+    std::memset(&s, 0, sizeof(s));
+    s.type = PTGPU_TRIANGLE;
+    ptgpu_vec *pv[3] = {&s.g.t.p1, &s.g.t.p2, &s.g.t.p3};
+    for (int k = 0; k < 3; ++k) {
+        const float *v = &obj.v[3 * (size_t)obj.tri[3 * t + k]];
+        pv[k]->x = v[0] * scale.x + pos.x;
+        pv[k]->y = v[1] * scale.y + pos.y;
+        pv[k]->z = v[2] * scale.z + pos.z;
+    }
+    s.e = e;
+    s.c = col;
+    s.refl = refl;
+    s.area = triangle_area(s.g.t.p1, s.g.t.p2, s.g.t.p3);
+    return s;
+}
+
+int parse_txt(const char *path, int width, int height, ptgpu_camera &cam, uint32_t &light_cnt, TxtSink &sink,
+              std::string &err) {
     FILE *f = std::fopen(path, "r");
     if (!f) { err = std::string("cannot open scene ") + path; return PTGPU_E_IO; }
     float gamma, sky[6];
     (void)std::fscanf(f, "gamma %f  sky1 %f %f %f  sky2 %f %f %f\n", &gamma, &sky[0], &sky[1],
                       &sky[2], &sky[3], &sky[4], &sky[5]);
-    ptgpu_camera &cam = sc.camera;
     std::memset(&cam, 0, sizeof(cam));
     int c = std::fscanf(f, "camera %f %f %f  %f %f %f\n", &cam.orig.x, &cam.orig.y, &cam.orig.z,
                         &cam.target.x, &cam.target.y, &cam.target.z);
@@ -184,7 +313,7 @@ int read_txt(const char *path, int width, int height, LoadedScene &sc, std::stri
             ptgpu_shape s = sphere_shape(r, cen, e, col, refl_from_material((int)mat));
             s.area = 4 * kPiF * r * r;
             if (!viszero(e)) ++lights;
-            sc.shapes.push_back(s);
+            sink.shape(s);
         } else if (!std::strcmp(kind, "triangle")) {
             ptgpu_shape s;
             std::memset(&s, 0, sizeof(s));
@@ -198,7 +327,7 @@ int read_txt(const char *path, int width, int height, LoadedScene &sc, std::stri
             s.refl = refl_from_material(imat);
             s.area = triangle_area(s.g.t.p1, s.g.t.p2, s.g.t.p3);
             if (!viszero(s.e)) ++lights;
-            sc.shapes.push_back(s);
+            sink.shape(s);
         } else if (!std::strcmp(kind, "model")) {
             char model[200];
             ptgpu_vec pos, scale, e, col;
@@ -217,25 +346,9 @@ int read_txt(const char *path, int width, int height, LoadedScene &sc, std::stri
                 if (!read_obj(alt.c_str(), obj, err2)) { std::fclose(f); return PTGPU_E_IO; }
                 err.clear();
             }
-            for (size_t t = 0; t + 2 < obj.tri.size(); t += 3) {
-                ptgpu_shape s;
-                std::memset(&s, 0, sizeof(s));
-                s.type = PTGPU_TRIANGLE;
-                ptgpu_vec *pv[3] = {&s.g.t.p1, &s.g.t.p2, &s.g.t.p3};
-                for (int k = 0; k < 3; ++k) {
-                    const float *v = &obj.v[3 * (size_t)obj.tri[t + k]];
-                    // scale then translate (displayfunc.cpp:402-410)
-                    pv[k]->x = v[0] * scale.x + pos.x;
-                    pv[k]->y = v[1] * scale.y + pos.y;
-                    pv[k]->z = v[2] * scale.z + pos.z;
-                }
-                s.e = e;
-                s.c = col;
-                s.refl = refl_from_material(imat);
-                s.area = triangle_area(s.g.t.p1, s.g.t.p2, s.g.t.p3);
-                if (!viszero(e)) ++lights;
-                sc.shapes.push_back(s);
-            }
+            const size_t ntri = obj.tri.size() / 3;
+            if (!viszero(e)) lights += (uint32_t)ntri;
+            sink.model(std::move(obj), pos, scale, e, col, refl_from_material(imat));
         } else {
             std::fclose(f);
             err = std::string("unknown object type ") + kind;
@@ -243,9 +356,41 @@ int read_txt(const char *path, int width, int height, LoadedScene &sc, std::stri
         }
     }
     std::fclose(f);
-    sc.light_cnt = lights;
-    sc.walllight = false;
+    light_cnt = lights;
     return PTGPU_OK;
+}
+
+struct AosSink : TxtSink {
+    std::vector<ptgpu_shape> &out;
+    explicit AosSink(std::vector<ptgpu_shape> &o) : out(o) {}
+    void shape(const ptgpu_shape &s) override { out.push_back(s); }
+    void model(Obj &&obj, ptgpu_vec pos, ptgpu_vec scale, ptgpu_vec e, ptgpu_vec col, int refl) override {
+        for (size_t t = 0; t < obj.tri.size() / 3; ++t) out.push_back(model_triangle(obj, t, pos, scale, e, col, refl));
+    }
+};
+
+struct CompactSink : TxtSink {
+    CompactScene &out;
+    explicit CompactSink(CompactScene &o) : out(o) {}
+    void shape(const ptgpu_shape &s) override {
+        if (out.segs.empty() || out.segs.back().model) out.segs.emplace_back();
+        out.segs.back().shapes.push_back(s);
+    }
+    void model(Obj &&obj, ptgpu_vec pos, ptgpu_vec scale, ptgpu_vec e, ptgpu_vec col, int refl) override {
+        if (obj.tri.empty()) return;
+        out.segs.emplace_back();
+        SceneSegment &g = out.segs.back();
+        g.model = true;
+        g.obj = std::move(obj);
+        g.pos = pos; g.scale = scale; g.e = e; g.c = col; g.refl = refl;
+    }
+};
+
+int read_txt(const char *path, int width, int height, LoadedScene &sc, std::string &err) {
+    AosSink sink(sc.shapes);
+    int st = parse_txt(path, width, height, sc.camera, sc.light_cnt, sink, err);
+    sc.walllight = false;
+    return st;
 }
 
 int read_scn(const char *path, int width, int height, LoadedScene &sc, std::string &err) {
@@ -289,6 +434,48 @@ int read_scene(const char *path, int width, int height, LoadedScene &out, std::s
     if (!std::strcmp(ext, "ply")) { err = ".ply scenes are not supported"; return PTGPU_E_INVAL; }
     err = std::string("unknown scene extension .") + ext;
     return PTGPU_E_INVAL;
+}
+
+int read_scene_compact(const char *path, int width, int height, CompactScene &out, std::string &err) {
+    out = CompactScene();
+    if (!path) { err = "null path"; return PTGPU_E_INVAL; }
+    const char *dot = std::strrchr(path, '.');
+    if (!dot) { err = "scene file has no extension"; return PTGPU_E_INVAL; }
+    const char *ext = dot + 1;
+    if (!std::strcmp(ext, "txt")) {
+        CompactSink sink(out);
+        int st = parse_txt(path, width, height, out.camera, out.light_cnt, sink, err);
+        out.walllight = false;
+        return st;
+    }
+    if (!std::strcmp(ext, "scn")) {
+        LoadedScene sc;
+        int st = read_scn(path, width, height, sc, err);
+        if (st != PTGPU_OK) return st;
+        out.camera = sc.camera;
+        out.light_cnt = sc.light_cnt;
+        out.walllight = sc.walllight;
+        if (!sc.shapes.empty()) {
+            out.segs.emplace_back();
+            out.segs.back().shapes = std::move(sc.shapes);
+        }
+        return PTGPU_OK;
+    }
+    if (!std::strcmp(ext, "ply")) { err = ".ply scenes are not supported"; return PTGPU_E_INVAL; }
+    err = std::string("unknown scene extension .") + ext;
+    return PTGPU_E_INVAL;
+}
+
+void add_wall_light(CompactScene &sc) {
+    LoadedScene w;
+    add_wall_light(w);
+    if (sc.segs.empty() || sc.segs.back().model) sc.segs.emplace_back();
+    std::vector<ptgpu_shape> &v = sc.segs.back().shapes;
+    v.insert(v.end(), w.shapes.begin(), w.shapes.end());
+}
+
+ptgpu_shape model_shape(const SceneSegment &g, size_t t) {
+    return model_triangle(g.obj, t, g.pos, g.scale, g.e, g.c, g.refl);
 }
 
 void add_wall_light(LoadedScene &sc) {     // smallptGPU.cpp:1448-1459

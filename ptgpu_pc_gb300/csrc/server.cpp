@@ -36,6 +36,7 @@
 
 #include "devbuf.h"
 #include "host.h"
+#include "ingest.h"
 #include "lbvh.h"
 
 using namespace ptgpu;
@@ -115,8 +116,12 @@ constexpr int64_t kSlotBytes = 64 + 48 + 4 + 32 + 48;
 constexpr int64_t kPixBytes = 12 + 4 + 8;
 
 struct SceneEntry {
-    // fixed when the scene is added
+    // fixed when the scene is added: shapes and light records in host memory,
+    // or a scene file that each build reads again (no host copy is kept)
     std::vector<ptgpu_shape> shapes;
+    std::string path;                    // scene file, when shapes is empty
+    int64_t n_shapes = 0;
+    int n_lights = 0;
     uint32_t light_cnt = 0;
     uint32_t build_flags = 0;
     std::vector<LightRec> lights;
@@ -174,6 +179,7 @@ struct ptgpu_server {
     // single-scene build scratch
     DevBuf s_shapes, s_verts, s_type, s_aabbs, s_keys, s_keys_alt, s_keys_tmp, s_vals_alt,
         s_vals_tmp, s_sorted, s_status, s_state, s_bb, s_arr, s_btn, s_btl, s_tcount, s_tcost;
+    IngestScratch ingest;                                         // scene files
     std::atomic<int> n_active{0};                                 // active.size() for readers
     // counters (guarded by mu)
     int64_t done_count = 0, builds = 0, evictions = 0, steps = 0;
@@ -237,8 +243,8 @@ int grow_lights(ptgpu_server *s, int64_t need) {
 
 void evict(ptgpu_server *s, int id) {
     SceneEntry &sc = scene_of(s, id);
-    s->shape_slots.release(sc.base, (int64_t)sc.shapes.size());
-    if (!sc.lights.empty()) s->light_slots.release(sc.light_base, (int64_t)sc.lights.size());
+    s->shape_slots.release(sc.base, sc.n_shapes);
+    if (sc.n_lights > 0) s->light_slots.release(sc.light_base, (int64_t)sc.n_lights);
     s->lru.erase(sc.lru);
     sc.resident = false;
     std::lock_guard<std::mutex> lk(s->mu);
@@ -276,18 +282,19 @@ bool alloc_pixels(ptgpu_server *s, int64_t n, int64_t *base) {
 // scratch buffers, then the traversal arrays written at the slot base).
 int build_scene(ptgpu_server *s, int id) {
     SceneEntry &sc = scene_of(s, id);
-    const int n = (int)sc.shapes.size();
+    const int n = (int)sc.n_shapes;
     int64_t base = 0;
     if (!alloc_shapes(s, n, &base)) return record_error(PTGPU_E_OOM, "scene does not fit the budget");
     int64_t lbase = 0;
-    if (!sc.lights.empty()) {
-        if (!s->light_slots.alloc((int64_t)sc.lights.size(), &lbase)) {
-            int st = grow_lights(s, (int64_t)sc.lights.size());
+    if (sc.n_lights > 0) {
+        if (!s->light_slots.alloc((int64_t)sc.n_lights, &lbase)) {
+            int st = grow_lights(s, (int64_t)sc.n_lights);
             if (st) return st;
-            s->light_slots.alloc((int64_t)sc.lights.size(), &lbase);
+            s->light_slots.alloc((int64_t)sc.n_lights, &lbase);
         }
-        SK(cudaMemcpyAsync(s->lights.buf.as<LightRec>() + lbase, sc.lights.data(),
-                           sc.lights.size() * sizeof(LightRec), cudaMemcpyHostToDevice, s->stream));
+        if (!sc.lights.empty())
+            SK(cudaMemcpyAsync(s->lights.buf.as<LightRec>() + lbase, sc.lights.data(),
+                               sc.lights.size() * sizeof(LightRec), cudaMemcpyHostToDevice, s->stream));
     }
     const size_t N = (size_t)n;
     SK(s->s_shapes.ensure(N * sizeof(ptgpu_shape)));
@@ -306,8 +313,20 @@ int build_scene(ptgpu_server *s, int id) {
     SK(s->s_arr.ensure(block_bound_count(n) * sizeof(uint32_t)));
     SK(s->s_btn.ensure((N - 1) * sizeof(ptgpu_bvh_node)));
     SK(s->s_btl.ensure(N * sizeof(ptgpu_bvh_node)));
-    SK(cudaMemcpyAsync(s->s_shapes.p, sc.shapes.data(), N * sizeof(ptgpu_shape), cudaMemcpyHostToDevice,
-                       s->stream));
+    if (sc.path.empty()) {
+        SK(cudaMemcpyAsync(s->s_shapes.p, sc.shapes.data(), N * sizeof(ptgpu_shape), cudaMemcpyHostToDevice,
+                           s->stream));
+    } else {   // a cold scene file: read again and expanded on the device
+        CompactScene cs;
+        std::string err;
+        int st = read_scene_compact(sc.path.c_str(), 1, 1, cs, err);
+        if (st != PTGPU_OK) return record_error(st, err);
+        if (cs.walllight) add_wall_light(cs);
+        if (cs.count() != sc.n_shapes || (int)compact_light_count(cs) != sc.n_lights)
+            return record_error(PTGPU_E_IO, "scene file changed since it was added: " + sc.path);
+        SK(ingest_compact(cs, s->s_shapes.as<ptgpu_shape>(), s->lights.buf.as<LightRec>() + lbase, s->ingest,
+                          s->stream));
+    }
     float4 *prims0 = s->prims0.buf.as<float4>() + 3 * base;
     SK(launch_unpack_shapes(s->s_shapes.as<ptgpu_shape>(), n, s->s_verts.as<float>(), s->s_type.as<uint8_t>(),
                             prims0, s->mats.buf.as<Material>() + base, s->stream));
@@ -387,7 +406,7 @@ void admit(ptgpu_server *s) {
         }
         SceneEntry &sc = scene_of(s, r->r.scene);
         const int64_t px = (int64_t)r->r.width * r->r.height;
-        const int64_t need = (int64_t)sc.shapes.size() * kSlotBytes + px * kPixBytes;
+        const int64_t need = sc.n_shapes * kSlotBytes + px * kPixBytes;
         if (need > s->budget) {
             { std::lock_guard<std::mutex> lk(s->mu); s->pending.pop_front(); }
             record_error(PTGPU_E_RANGE, "request can never fit the budget");
@@ -459,11 +478,11 @@ int step(ptgpu_server *s) {
         r.max_depth = q.r.max_depth ? q.r.max_depth : PTGPU_MAX_DEPTH;
         r.start_sample = q.done_passes;
         r.root = (int32_t)sc.base;
-        r.n_shapes = (int32_t)sc.shapes.size();
-        r.skip = (int32_t)(sc.base + (int64_t)sc.shapes.size() - 1);
+        r.n_shapes = (int32_t)sc.n_shapes;
+        r.skip = (int32_t)(sc.base + sc.n_shapes - 1);
         r.shape0 = (int32_t)sc.base;
         r.light_first = (int32_t)sc.light_base;
-        r.n_lights = (int32_t)sc.lights.size();
+        r.n_lights = (int32_t)sc.n_lights;
         r.pix_off = q.pix_base;
         std::memcpy(r.root_box, sc.root_box, sizeof(r.root_box));
         start[k + 1] = start[k] + (int64_t)q.r.width * q.r.height;
@@ -620,6 +639,7 @@ int ptgpu_server_destroy(ptgpu_server *s) {
                       &s->s_vals_alt, &s->s_vals_tmp, &s->s_sorted, &s->s_status, &s->s_state,
                       &s->s_bb, &s->s_arr, &s->s_btn, &s->s_btl, &s->s_tcount, &s->s_tcost};
     for (DevBuf *d : bufs) d->release();
+    s->ingest.release();
     cudaStreamDestroy(s->stream);
     delete s;
     return PTGPU_OK;
@@ -636,9 +656,36 @@ int ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t 
             return record_error(PTGPU_E_INVAL, "shape " + std::to_string(i) + " has an unknown type");
     auto e = std::make_unique<SceneEntry>();
     e->shapes.assign(shapes, shapes + n);
+    e->n_shapes = n;
     e->light_cnt = light_cnt;
     e->build_flags = build_flags;
     make_lights(shapes, n, light_cnt, e->lights);
+    e->n_lights = (int)e->lights.size();
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->scenes.push_back(std::move(e));
+    if (scene) *scene = (int32_t)s->scenes.size() - 1;
+    return PTGPU_OK;
+}
+
+int ptgpu_server_add_scene_file(ptgpu_server *s, const char *path, uint32_t build_flags, int32_t *scene) {
+    if (!s || !path) return record_error(PTGPU_E_INVAL, "null argument");
+    if (build_flags & PTGPU_FLAG_MORTON_DELTA) return record_error(PTGPU_E_INVAL, "build flag not supported");
+    // read once to check the file and count its shapes and lights; the
+    // scene is read again whenever it has to be built
+    CompactScene cs;
+    std::string err;
+    int st = read_scene_compact(path, 1, 1, cs, err);
+    if (st != PTGPU_OK) return record_error(st, err);
+    if (cs.walllight) add_wall_light(cs);
+    const int64_t n = cs.count();
+    if (n < 2) return record_error(PTGPU_E_INVAL, "a served scene needs at least 2 shapes");
+    if (n >= (1 << 29)) return record_error(PTGPU_E_RANGE, "scene too large");
+    auto e = std::make_unique<SceneEntry>();
+    e->path = path;
+    e->n_shapes = n;
+    e->light_cnt = cs.light_cnt;
+    e->n_lights = (int)compact_light_count(cs);
+    e->build_flags = build_flags;
     std::lock_guard<std::mutex> lk(s->mu);
     s->scenes.push_back(std::move(e));
     if (scene) *scene = (int32_t)s->scenes.size() - 1;

@@ -255,3 +255,84 @@ def scene_from_spec(spec):
     shapes, lc, cam = icosphere_scene(level=spec["level"], seed=spec["seed"] % 1000,
                                       n_tris=spec["n_tris"])
     return shapes, lc, cam
+
+
+# ---------------------------------------------------------------------------
+# OBJ model and .txt scene files (scene ingestion)
+# ---------------------------------------------------------------------------
+def write_obj_model(path, n_tris, seed=3, block=64):
+    """Writes a seeded OBJ model of about n_tris triangles and returns (path,
+    vertices (nv, 3) float32, triangles (nt, 3) int32) as a reader must see
+    them.  Vertices come in blocks, each followed by faces on the vertices
+    defined so far, in every face form the reader takes: "i", "i/j", "i//k",
+    "i/j/k", negative (relative) indices and quads (fanned into two
+    triangles); plus comments, vt / vn lines, leading blanks, CRLF and lone
+    CR line ends.  Values are written with 9 significant digits, which read
+    back to the same float32."""
+    rng = np.random.default_rng(seed)
+    out, verts, tris = [], [], []
+    nv = 0
+    ends = ("\n", "\n", "\n", "\r\n", "\r")
+    n_faces = 2 * block
+    while sum(len(t) for t in tris) < n_tris:
+        v = (rng.random((block, 3)) * 100.0 - 50.0).astype(np.float32)
+        lead = rng.random(block) < 0.05
+        vend = rng.integers(len(ends), size=block)
+        for x, ld, en in zip(v.tolist(), lead, vend):
+            out.append("%sv %.9g %.9g %.9g%s" % (" " if ld else "", x[0], x[1], x[2], ends[en]))
+        verts.append(v)
+        nv += block
+        if rng.random() < 0.3:
+            out.append("# block %d\nvt 0.5 0.5\nvn 0 0 1\n" % nv)
+        # distinct corners: a start and up to three steps below nv/4, mod nv
+        k = np.where(rng.random(n_faces) < 0.2, 4, 3)
+        steps = rng.integers(1, max(2, nv // 4), (n_faces, 3))
+        start = rng.integers(0, nv, n_faces)
+        idx = np.concatenate([start[:, None], start[:, None] + np.cumsum(steps, axis=1)], axis=1) % nv
+        forms = rng.integers(5, size=n_faces)
+        fend = rng.integers(len(ends), size=n_faces)
+        for q, kk, form, en in zip(idx.tolist(), k.tolist(), forms.tolist(), fend.tolist()):
+            q = q[:kk]
+            if form == 0:
+                toks = ["%d" % (i + 1) for i in q]
+            elif form == 1:
+                toks = ["%d/1" % (i + 1) for i in q]
+            elif form == 2:
+                toks = ["%d//1" % (i + 1) for i in q]
+            elif form == 3:
+                toks = ["%d/1/1" % (i + 1) for i in q]
+            else:
+                toks = ["%d" % (i - nv) for i in q]     # relative: -1 is the last vertex
+            out.append("f " + " ".join(toks) + ends[en])
+        tri = np.stack([idx[:, 0], idx[:, 1], idx[:, 2]], axis=1)
+        quad = np.stack([idx[k == 4, 0], idx[k == 4, 2], idx[k == 4, 3]], axis=1)
+        # fanned triangles in file order: each face's first, then a quad's second
+        order = np.concatenate([np.flatnonzero(np.ones(n_faces, bool)) * 2,
+                                np.flatnonzero(k == 4) * 2 + 1])
+        both = np.concatenate([tri, quad])
+        tris.append(both[np.argsort(order, kind="stable")])
+    out.append("\n")      # the reader drops the line before the final byte
+    with open(path, "w", newline="") as f:
+        f.write("".join(out))
+    return path, np.concatenate(verts), np.concatenate(tris).astype(np.int32)
+
+
+def write_model_scene(directory, n_tris, seed=4):
+    """A .txt scene (ReadTxt format) mixing spheres, triangle lines and two
+    OBJ models of about n_tris/2 triangles each, one of them emitting;
+    returns its path."""
+    import os
+    half = max(1, n_tris // 2)
+    m1, _, _ = write_obj_model(os.path.join(str(directory), "m1.obj"), half, seed=seed)
+    m2, _, _ = write_obj_model(os.path.join(str(directory), "m2.obj"), half, seed=seed + 1)
+    path = os.path.join(str(directory), "scene.txt")
+    with open(path, "w") as f:
+        f.write("gamma 2.2  sky1 0 0 0  sky2 0 0 0\ncamera 0 10 120  0 0 0\nmaterials 1\n"
+                "matte 0.5 0.5 0.5  0.1\nobjects 6\n"
+                "sphere 5  0 30 0  4 4 4  0 0 0  0\n"
+                "triangle  -60 -50 -60  60 -50 -60  0 -50 60  0 0 0  0.7 0.7 0.7  0\n"
+                "model %s  -20 0 0  0.3 0.3 0.3  0 0 0  0.8 0.6 0.4  0\n"
+                "sphere 3  20 20 20  0 0 0  0.9 0.9 0.9  2\n"
+                "model %s  20 0 0  0.2 0.2 0.2  1.5 1.5 1.5  0.5 0.5 0.5  1\n"
+                "triangle  -60 60 -60  60 60 -60  0 60 60  0 0 0  0.7 0.7 0.7  0\n" % (m1, m2))
+    return path

@@ -83,6 +83,46 @@ void shim_scene_get(ptgpu_shape *out, ptgpu_camera *cam) {
     *cam = g_scene.camera;
 }
 
+// read_obj with a given number of host threads; returns 1 on success and
+// the counts, or 0 with the error text
+static ptgpu::Obj g_obj;
+int shim_read_obj(const char *path, int threads, int64_t *nv, int64_t *ntri, char *err, int errlen) {
+    std::string e;
+    g_obj = ptgpu::Obj();
+    const bool ok = ptgpu::read_obj(path, g_obj, e, threads);
+    *nv = (int64_t)(g_obj.v.size() / 3);
+    *ntri = (int64_t)(g_obj.tri.size() / 3);
+    std::strncpy(err, e.c_str(), errlen - 1);
+    err[errlen - 1] = 0;
+    return ok ? 1 : 0;
+}
+void shim_obj_get(float *v, int32_t *tri) {
+    std::memcpy(v, g_obj.v.data(), g_obj.v.size() * sizeof(float));
+    std::memcpy(tri, g_obj.tri.data(), g_obj.tri.size() * sizeof(int32_t));
+}
+
+// read_scene_compact (+ wall light), its segments expanded in order
+static std::vector<ptgpu_shape> g_compact;
+int shim_read_scene_compact(const char *path, int w, int h, int *n, int *light_cnt, int *segs) {
+    ptgpu::CompactScene sc;
+    std::string e;
+    int st = ptgpu::read_scene_compact(path, w, h, sc, e);
+    if (st != PTGPU_OK) return st;
+    if (sc.walllight) ptgpu::add_wall_light(sc);
+    g_compact.clear();
+    for (const ptgpu::SceneSegment &g : sc.segs) {
+        if (!g.model) g_compact.insert(g_compact.end(), g.shapes.begin(), g.shapes.end());
+        else for (int64_t t = 0; t < g.count(); ++t) g_compact.push_back(ptgpu::model_shape(g, (size_t)t));
+    }
+    *n = (int)g_compact.size();
+    *light_cnt = (int)sc.light_cnt;
+    *segs = (int)sc.segs.size();
+    return PTGPU_OK;
+}
+void shim_compact_get(ptgpu_shape *out) {
+    std::memcpy(out, g_compact.data(), g_compact.size() * sizeof(ptgpu_shape));
+}
+
 void shim_update_camera(ptgpu_camera *cam) { ptgpu::update_camera(cam); }
 
 void shim_make_seeds(uint64_t m, uint32_t *s, uint32_t n) { ptgpu::make_seeds(m, s, n); }

@@ -32,6 +32,10 @@ def shim(tmp_path_factory):
                                   ctypes.c_char_p, ctypes.c_int]
     L.shim_scene_get.argtypes = [vp, vp]
     L.shim_update_camera.argtypes = [vp]
+    L.shim_read_obj.argtypes = [ctypes.c_char_p, ctypes.c_int, vp, vp, ctypes.c_char_p, ctypes.c_int]
+    L.shim_obj_get.argtypes = [vp, vp]
+    L.shim_read_scene_compact.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp]
+    L.shim_compact_get.argtypes = [vp]
     L.shim_make_seeds.argtypes = [ctypes.c_uint64, vp, ctypes.c_uint32]
     return L
 
@@ -197,3 +201,72 @@ def test_loader_matches_reference_loader(shim):
             a, b = a[tri], b[tri]
         assert a.tobytes() == b.tobytes(), f
     assert cam.tobytes()[:40] == z["camera"].tobytes()[:40]
+
+
+def _read_obj(shim, path, threads):
+    nv, nt = ctypes.c_int64(), ctypes.c_int64()
+    err = ctypes.create_string_buffer(256)
+    ok = shim.shim_read_obj(str(path).encode(), threads, ctypes.byref(nv), ctypes.byref(nt), err, 256)
+    if not ok:
+        return None, err.value.decode()
+    v = np.zeros(3 * nv.value, np.float32)
+    t = np.zeros(3 * nt.value, np.int32)
+    shim.shim_obj_get(_p(v), _p(t))
+    return (v.reshape(-1, 3), t.reshape(-1, 3)), ""
+
+
+def test_obj_reader_threads_agree(shim, tmp_path):
+    """The OBJ reader cut into runs of lines on several threads gives the
+    one-thread result: same vertices (as written, float32), same fanned
+    triangles in file order, with relative indices, v/vt/vn tokens, comments,
+    CRLF and lone-CR line ends, and the final-line rule."""
+    path, verts, tris = scenes.write_obj_model(tmp_path / "big.obj", 200_000, seed=3)
+    one, e1 = _read_obj(shim, path, 1)
+    many, e2 = _read_obj(shim, path, 16)
+    assert one is not None and many is not None, (e1, e2)
+    assert one[0].tobytes() == many[0].tobytes() and one[1].tobytes() == many[1].tobytes()
+    assert np.array_equal(one[0], verts) and np.array_equal(one[1], tris)
+    for threads in (2, 3, 7):
+        got, _ = _read_obj(shim, path, threads)
+        assert got[1].tobytes() == one[1].tobytes()
+
+
+def test_obj_reader_errors_in_file_order(shim, tmp_path):
+    """Errors are those of a sequential read: the first malformed line
+    decides, and a face may only use vertices defined above it."""
+    body = "".join("v %d 0 0\n" % i for i in range(50_000))
+    bad_face_then_vertex = tmp_path / "a.obj"
+    bad_face_then_vertex.write_text(body + "f 1 2 60000\n" + body + "v 1 2\n" + "f 1 2 3\n\n")
+    for threads in (1, 8):
+        got, err = _read_obj(shim, bad_face_then_vertex, threads)
+        assert got is None and err.startswith("malformed face"), err
+    bad_vertex = tmp_path / "b.obj"
+    bad_vertex.write_text(body + "v 1 x 2\n" + body + "f 1 2 3\n\n")
+    for threads in (1, 8):
+        got, err = _read_obj(shim, bad_vertex, threads)
+        assert got is None and err.startswith("malformed vertex"), err
+    forward = tmp_path / "c.obj"
+    forward.write_text("f 1 2 3\n" + body + "\n")
+    for threads in (1, 8):
+        got, err = _read_obj(shim, forward, threads)
+        assert got is None and err.startswith("malformed face"), err
+
+
+def test_compact_scene_expands_to_read_scene(shim, tmp_path):
+    """The compact scene form (shape runs + models kept as vertex and index
+    arrays) expands, segment by segment, to read_scene's shapes byte for byte."""
+    scene = scenes.write_model_scene(tmp_path, 30_000, seed=4)
+    n, lc, wl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    err = ctypes.create_string_buffer(256)
+    assert shim.shim_read_scene(str(scene).encode(), 32, 24, ctypes.byref(n), ctypes.byref(lc),
+                                ctypes.byref(wl), err, 256) == 0, err.value
+    ref = np.zeros(n.value, abi.SHAPE)
+    cam = np.zeros(1, abi.CAMERA)
+    shim.shim_scene_get(_p(ref), _p(cam))
+    n2, lc2, segs = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert shim.shim_read_scene_compact(str(scene).encode(), 32, 24, ctypes.byref(n2), ctypes.byref(lc2),
+                                        ctypes.byref(segs)) == 0
+    assert n2.value == n.value and lc2.value == lc.value and segs.value >= 4
+    got = np.zeros(n2.value, abi.SHAPE)
+    shim.shim_compact_get(_p(got))
+    assert got.tobytes() == ref.tobytes()
