@@ -500,7 +500,7 @@ def main():
         ctx.reset()
         starts[i].record(stream)
         ctx.render_async(SPP)
-        launches += 1
+        launches += 4        # k_render, then the next frame's hand-out order (3 kernels)
         ends[i].record(stream)
     ctx.synchronize()
     torch.cuda.synchronize()

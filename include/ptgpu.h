@@ -123,6 +123,10 @@ typedef struct {
                                          left-to-right order of OpenCL/clang)   */
 #define PTGPU_FLAG_KD_HOST       0x20 /* build the KD tree with the sequential host
                                          code instead of the GPU (same tree)     */
+#define PTGPU_FLAG_ROW_ORDER     0x40 /* hand pixels out in row order on every
+                                         frame (default: from the second frame on,
+                                         in decreasing work of the frame before;
+                                         results are the same either way)      */
 /* build flag field: rounds of the treelet stage (bits 8-11; 0 = one round,
  * the single launch of CLBVH::optimize, CLBVH.cpp:318-350).  Each round runs
  * over the tree the previous one left; Karras & Aila use three. */

@@ -105,6 +105,7 @@ FLAG_TREELET = 0x4
 FLAG_ARGS_RTL = 0x8
 FLAG_WIDE_TRAVERSAL = 0x10
 FLAG_KD_HOST = 0x20
+FLAG_ROW_ORDER = 0x40
 
 
 def treelet_sweeps(n):

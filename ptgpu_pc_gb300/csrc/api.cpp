@@ -108,6 +108,8 @@ struct ptgpu_ctx {
     // rendering
     int w = 0, h = 0;
     DevBuf d_colors, d_pixels, d_seeds, d_err, d_pixctr, d_wf;
+    DevBuf d_cost, d_order, d_order_scr;   // per-pixel work, next hand-out order
+    bool order_valid = false;
     uint32_t *h_pixels = nullptr;
     int current_sample = 0;
     ptgpu_camera cam{};
@@ -231,6 +233,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_tcount, &c->d_tcost, &c->d_aabbs,
                       &c->d_nodes, &c->d_nodes4, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_wf, &c->d_rays, &c->d_t,
+                      &c->d_cost, &c->d_order, &c->d_order_scr,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
     c->ingest.release();
@@ -679,7 +682,21 @@ static int enqueue_render(ptgpu_ctx *c, uint32_t passes, unsigned long long *sta
         const int grid = c->sm_count * 12;
         CK(launch_wavefront(w, (int)passes * (c->max_depth + 1), grid, c->stream));
     } else {
+        // pixels handed out in decreasing work of the previous frame, so the
+        // frame ends on short pixel chains (first frame: row order)
+        const int npx = c->w * c->h;
+        CK(c->d_cost.ensure((size_t)npx * sizeof(uint32_t)));
+        CK(c->d_order.ensure((size_t)npx * sizeof(int32_t)));
+        CK(c->d_order_scr.ensure(2 * kOrderScratchWords * sizeof(uint32_t)));
+        const bool reorder = !(c->flags & PTGPU_FLAG_ROW_ORDER);
+        a.order = reorder && c->order_valid ? c->d_order.as<int32_t>() : nullptr;
+        a.cost = reorder ? c->d_cost.as<uint32_t>() : nullptr;
         CK(launch_render(a, c->block, c->stream));
+        if (reorder) {
+            CK(launch_pixel_order(c->d_cost.as<uint32_t>(), c->d_order.as<int32_t>(),
+                                  c->d_order_scr.as<uint32_t>(), npx, c->stream));
+            c->order_valid = true;
+        }
     }
     c->current_sample += (int)passes;
     return PTGPU_OK;

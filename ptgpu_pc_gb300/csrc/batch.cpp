@@ -338,13 +338,11 @@ int ptgpu_batch_build(ptgpu_batch *b, uint32_t flags) {
     BK(launch_lbvh_build_seg(lb, (int)n, sb, b->sm_count, b->stream));
     if (flags & PTGPU_FLAG_TREELET) {
         const int sweeps = ((flags >> 8) & 0xF) ? (int)((flags >> 8) & 0xF) : 1;
-        BK(b->d_tcount.ensure(max_n * sizeof(int)));
-        BK(b->d_tcost.ensure(max_n * sizeof(float)));
-        for (int s = 0; s < S; ++s) {
-            const int off = b->seg_off[s], ns = b->seg_off[s + 1] - off;
-            BK(launch_treelet(lb.btn + (off - s), lb.btl + off, ns, b->d_tcount.as<int>(),
+        BK(b->d_tcount.ensure((size_t)n * sizeof(int)));
+        BK(b->d_tcost.ensure((size_t)n * sizeof(float)));
+        // every scene's tree in one launch per round
+        BK(launch_treelet_seg(lb.btn, lb.btl, b->d_seg_off.as<int32_t>(), S, (int)n, b->d_tcount.as<int>(),
                               b->d_tcost.as<float>(), sweeps, b->stream));
-        }
     }
     BK(cudaEventRecord(b->ev1, b->stream));
     uint32_t err_word = 0;

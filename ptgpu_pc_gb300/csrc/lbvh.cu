@@ -1443,6 +1443,118 @@ __global__ void k_treelet_finish(ptgpu_bvh_node *btn, int n, const float *cost) 
     p.area = area6(b);
 }
 
+// The treelet rounds of every segment's tree in one launch per round (the
+// batched build): segment g's tree has n_g = seg_off[g+1] - seg_off[g]
+// leaves, its leaves at btl + seg_off[g] and its internal nodes, counters and
+// costs at seg_off[g] - g, all indices inside segment-local.  Segments with
+// fewer than 3 leaves are left alone, as launch_treelet leaves such a tree.
+__device__ __forceinline__ int internal_segment(const int32_t *seg_off, int n_segs, int i) {
+    int lo = 0, hi = n_segs - 1;          // the last g with seg_off[g] - g <= i
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (seg_off[mid] - mid <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_treelet_prepare_seg(ptgpu_bvh_node *btn, const int32_t *__restrict__ seg_off, int n_segs,
+                                      int n_internal, int *counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal) return;
+    const int g = internal_segment(seg_off, n_segs, i);
+    if (seg_off[g + 1] - seg_off[g] < 3) return;
+    ptgpu_bvh_node &p = btn[i];
+    const bool ll = p.nLeft == p.min, rl = p.nRight == p.max;
+    p.min = ll ? p.nLeft : -1;
+    p.max = rl ? p.nRight : -1;
+    counters[i] = 0;
+}
+
+__global__ void k_treelet_finish_seg(ptgpu_bvh_node *btn, const int32_t *__restrict__ seg_off, int n_segs,
+                                     int n_internal, const float *cost) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal) return;
+    const int g = internal_segment(seg_off, n_segs, i);
+    if (seg_off[g + 1] - seg_off[g] < 3) return;
+    ptgpu_bvh_node &p = btn[i];
+    float b[6] = {p.bound.min_x, p.bound.max_x, p.bound.min_y, p.bound.max_y, p.bound.min_z,
+                  p.bound.max_z};
+    p.cost = cost[i];
+    p.area = area6(b);
+}
+
+__global__ void __launch_bounds__(kTreeletThreads) k_treelet_seg(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl,
+                                                                  const int32_t *__restrict__ seg_off, int n_segs,
+                                                                  int n_total, int *counters, float *cost) {
+    __shared__ TreeletSmem s_tl[kTreeletThreads / 32];
+    TreeletSmem &sm = s_tl[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int g = 0, off = 0, n = 0;
+    if (k < n_total) {
+        g = (int)segment_of(seg_off, n_segs, k);
+        off = seg_off[g];
+        n = seg_off[g + 1] - off;
+    }
+    // this lane's tree: internal nodes, counters and costs at off - g
+    ptgpu_bvh_node *tn = btn + (off - g), *tl = btl + off;
+    int *tc = counters + (off - g);
+    float *tcost = cost + (off - g);
+    int node = (k < n_total && n >= 3) ? tl[k - off].nParent : -1;
+    bool active = node >= 0 && node < n - 1;
+    while (__any_sync(0xffffffffu, active)) {
+        bool mine = false;
+        float my_cost = 0.f;
+        if (active) {
+            __threadfence();
+            if (atomicAdd(&tc[node], 1) == 0) {
+                active = false;                    // the second arrival goes on
+            } else {
+                __threadfence();
+                const NodeL p = load_node(tn, node);
+                int lr = p.min == p.nLeft ? -(p.nLeft + 1) : p.nLeft;
+                int rr = p.max == p.nRight ? -(p.nRight + 1) : p.nRight;
+                float b[6];
+                ref_bound6(node, tn, tl, b);
+                my_cost = 1.2f * area6(b) + ref_cost(lr, tcost, tl) + ref_cost(rr, tcost, tl);
+                tcost[node] = my_cost;
+                mine = true;
+            }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, mine);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const int root = __shfl_sync(0xffffffffu, node, src);
+            const float rc = __shfl_sync(0xffffffffu, my_cost, src);
+            const int sg = __shfl_sync(0xffffffffu, g, src);
+            const int so = __shfl_sync(0xffffffffu, off, src);
+            treelet_warp(root, rc, btn + (so - sg), btl + so, cost + (so - sg), sm, lane);
+            __syncwarp();
+        }
+        if (mine) {
+            __threadfence();
+            if (node == 0) active = false;
+            else node = load_node(tn, node).nParent;
+            if (node < 0 || node >= n - 1) active = false;
+        }
+    }
+}
+
+cudaError_t launch_treelet_seg(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, const int32_t *seg_off, int n_segs,
+                               int n_total, int *counters, float *cost, int sweeps, cudaStream_t s) {
+    const int n_internal = n_total - n_segs;
+    if (n_internal <= 0) return cudaSuccess;
+    k_treelet_prepare_seg<<<(n_internal + 255) / 256, 256, 0, s>>>(btn, seg_off, n_segs, n_internal, counters);
+    for (int it = 0; it < sweeps; ++it) {
+        if (it > 0) cudaMemsetAsync(counters, 0, sizeof(int) * (size_t)n_internal, s);
+        k_treelet_seg<<<(n_total + kTreeletThreads - 1) / kTreeletThreads, kTreeletThreads, 0, s>>>(
+            btn, btl, seg_off, n_segs, n_total, counters, cost);
+    }
+    k_treelet_finish_seg<<<(n_internal + 255) / 256, 256, 0, s>>>(btn, seg_off, n_segs, n_internal, cost);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int *counters,
                            float *cost, int sweeps, cudaStream_t s) {
     if (n < 3) return cudaSuccess;

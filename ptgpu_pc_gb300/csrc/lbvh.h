@@ -67,6 +67,11 @@ cudaError_t launch_lbvh_build_seg(const LbvhBuffers &b, int n_total, const SegBu
                                   int sm_count, cudaStream_t s);
 cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int *counters,
                            float *cost, int sweeps, cudaStream_t s);
+// The same rounds for every segment of a batched build in one launch each
+// (segment g: leaves at btl + seg_off[g], internal nodes / counters / costs
+// at seg_off[g] - g); counters and cost hold n_total - n_segs entries.
+cudaError_t launch_treelet_seg(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, const int32_t *seg_off, int n_segs,
+                               int n_total, int *counters, float *cost, int sweeps, cudaStream_t s);
 // node_base / shape_base: added to the child references and shape ids
 // written (a segment's place in the shared arrays of a batch; 0 otherwise)
 cudaError_t launch_abi_to_trace(const ptgpu_bvh_node *btn, const ptgpu_bvh_node *btl, int n,
@@ -113,6 +118,12 @@ struct RenderArgs {
     uint32_t *seeds;            // 2*W*H
     unsigned long long *stats;  // optional traversal counters (6 words)
     unsigned int *pixel_counter;// next pixel to hand out (zeroed per launch)
+    // single-scene renders: the hand-out order (a permutation of the pixels;
+    // null: row order) and each pixel's measured work, written as it finishes
+    // (null: not measured).  Which lane renders a pixel when does not change
+    // its result, so the order only decides how the frame's tail packs.
+    const int32_t *order;
+    uint32_t *cost;
     int32_t max_ctas;           // grid cap (resident CTAs); 0 = one lane per pixel
     int32_t refill;             // 32nds of a warp's live lanes that wait before it
                                 // shades (0: the default)
@@ -124,6 +135,12 @@ struct RenderArgs {
     int32_t n_scenes;
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
+// The next frame's hand-out order from this frame's per-pixel work: pixels in
+// decreasing work (logarithmic classes, 8 per power of two; any order inside
+// a class), so the longest pixel chains start first and the frame ends on
+// short ones.  scratch: 2 * kOrderScratchWords words.
+constexpr int kOrderScratchWords = 1024;
+cudaError_t launch_pixel_order(const uint32_t *cost, int32_t *order, uint32_t *scratch, int npx, cudaStream_t s);
 // A batched render (binary nodes; stack 32, 64 or 128 entries) on `grid` resident
 // CTAs from render_batch_grid; the launch only enqueues stream work (the
 // pixel counter's reset and the kernel), so it can be captured in a graph.

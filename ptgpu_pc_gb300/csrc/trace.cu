@@ -24,6 +24,7 @@
 // contributions are summed in light order as in the reference, and every
 // query visits its nodes in the same order whether it runs in one go or in
 // steps.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -90,6 +91,15 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     const int refill = a.refill > 0 ? a.refill : PTGPU_RENDER_REFILL;
     int state = ST_NEED;
     int gid = 0, passes_done = 0, depth = 0, li = 0, specular = 1;
+    // a pixel's work for the next frame's hand-out order: SM clock cycles from
+    // taking the pixel to finishing it (PTGPU_ORDER_CLOCK=0: loop rounds, which
+    // ordered the benchmark frame no better than row order; cycles: 29.5 ->
+    // 28.8 ms)
+#ifndef PTGPU_ORDER_CLOCK
+#define PTGPU_ORDER_CLOCK 1
+#endif
+    uint32_t work = 0;   // loop rounds spent on the lane's pixel
+    uint32_t t_pix = 0;  // SM clock when the lane took its pixel
     int sc = 0;          // BATCH: the lane's scene (hand-out order)
     uint32_t s0 = 0, s1 = 0;
     f3 col = mk3(0.f, 0.f, 0.f), rad = col, tp = col, hp = col, nl = col;
@@ -152,8 +162,10 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                         sc = lo;
                         gid = (int)(g - s_start[lo]);
                     } else {
-                        gid = (int)g;
+                        gid = a.order ? __ldg(a.order + g) : (int)g;
                     }
+                    work = 0;
+                    if (PTGPU_ORDER_CLOCK) t_pix = (uint32_t)clock();
                     const uint2 sd = reinterpret_cast<const uint2 *>(a.seeds)[pix_off() + gid];
                     s0 = sd.x; s1 = sd.y;
                     if (start_sample() > 0) {
@@ -168,6 +180,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
             }
         }
         if (__all_sync(0xffffffffu, state == ST_DONE)) break;
+        ++work;
 
         // ---- lanes without a query: produce the next one
         if (!trav && !fin) {
@@ -407,6 +420,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                 a.pixels[po + gid] = to_int(col.x) | (to_int(col.y) << 8) | (to_int(col.z) << 16) |
                                      0xff000000u;
                 reinterpret_cast<uint2 *>(a.seeds)[po + gid] = make_uint2(s0, s1);
+                if (!BATCH && a.cost) a.cost[gid] = PTGPU_ORDER_CLOCK ? (uint32_t)clock() - t_pix : work;
                 state = ST_NEED;
             }
         }
@@ -429,6 +443,79 @@ static int resident_grid(const void *kernel, int block, int max_ctas) {
     int resident = per_sm * sms;
     if (max_ctas > 0 && resident > max_ctas) resident = max_ctas;
     return resident;
+}
+
+// ---- hand-out order of the next frame -----------------------------------
+// class of a pixel's work: 0 for the most, kOrderClasses - 1 for the least
+// (kOrderSub classes per power of two)
+#ifndef PTGPU_ORDER_SUBBITS
+#define PTGPU_ORDER_SUBBITS 3
+#endif
+constexpr int kOrderSub = 1 << PTGPU_ORDER_SUBBITS;
+constexpr int kOrderClasses = 32 * kOrderSub;
+static_assert(kOrderClasses <= kOrderScratchWords, "order scratch");
+__device__ __forceinline__ int work_class(uint32_t w) {
+    const uint32_t v = w + 1u;
+    const int lz = 31 - __clz((int)v);
+    const int sub = lz >= PTGPU_ORDER_SUBBITS ? (int)((v >> (lz - PTGPU_ORDER_SUBBITS)) & (kOrderSub - 1))
+                                              : (int)((v << (PTGPU_ORDER_SUBBITS - lz)) & (kOrderSub - 1));
+    return kOrderClasses - 1 - (kOrderSub * lz + sub);
+}
+
+__global__ void k_order_hist(const uint32_t *__restrict__ cost, int npx, uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[kOrderClasses];
+    for (int i = threadIdx.x; i < kOrderClasses; i += blockDim.x) h[i] = 0u;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[work_class(__ldg(cost + i))], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kOrderClasses; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// hist[0..C-1] -> exclusive offsets in hist[C..2C-1] (one block of C threads)
+__global__ void k_order_scan(uint32_t *hist) {
+    __shared__ uint32_t t[kOrderClasses];
+    const int c = threadIdx.x;
+    t[c] = hist[c];
+    __syncthreads();
+    for (int o = 1; o < kOrderClasses; o <<= 1) {      // inclusive Hillis-Steele scan
+        const uint32_t v = c >= o ? t[c - o] : 0u;
+        __syncthreads();
+        t[c] += v;
+        __syncthreads();
+    }
+    hist[kOrderClasses + c] = t[c] - hist[c];
+}
+
+__global__ void k_order_scatter(const uint32_t *__restrict__ cost, int npx, uint32_t *__restrict__ offs,
+                                int32_t *__restrict__ order) {
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < npx; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool ok = i < npx;
+        const int c = ok ? work_class(__ldg(cost + i)) : kOrderClasses + lane;   // distinct dummies
+        const unsigned peers = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(peers) - 1;
+        uint32_t pos = 0;
+        if (ok && lane == leader) pos = atomicAdd(&offs[c], (uint32_t)__popc(peers));
+        pos = __shfl_sync(0xffffffffu, pos, leader);
+        if (ok) order[pos + __popc(peers & ((1u << lane) - 1u))] = i;
+    }
+}
+
+cudaError_t launch_pixel_order(const uint32_t *cost, int32_t *order, uint32_t *scratch, int npx, cudaStream_t s) {
+    if (npx <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, kOrderClasses * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::min((npx + 255) / 256, sms * 4);
+    k_order_hist<<<grid, 256, 0, s>>>(cost, npx, scratch);
+    k_order_scan<<<1, kOrderClasses, 0, s>>>(scratch);
+    k_order_scatter<<<grid, 256, 0, s>>>(cost, npx, scratch + kOrderClasses, order);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s) {

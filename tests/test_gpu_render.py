@@ -102,6 +102,19 @@ def test_progressive_equals_single_call(built_lib, orc):
     assert (a[1] == b[1]).all() and (a[2] == b[2]).all()
 
 
+def test_handout_order_keeps_results(built_lib, orc):
+    """Frames after the first hand pixels out in decreasing work of the frame
+    before; results do not depend on the order: 1+1+1+1 passes in four calls
+    (three of them reordered) == 4 passes in one call (row order)."""
+    shapes, lc, cam = scenes.icosphere_scene(level=4)
+    w, h = 160, 120
+    seeds = orc.make_seeds(5, 2 * w * h)
+    a = _gpu_render(shapes, lc, cam, w, h, seeds, 4, abi.ACCEL_BVH)
+    b = _gpu_render(shapes, lc, cam, w, h, seeds, 4, abi.ACCEL_BVH, chunks=[1, 1, 1, 1])
+    assert a[0].tobytes() == b[0].tobytes()
+    assert (a[1] == b[1]).all() and (a[2] == b[2]).all()
+
+
 def test_render_obj_model_fixture(built_lib, orc):
     """The reference's own OBJ scene, loaded by the reference loader when the
     golden fixture was made, rendered in all three modes."""
