@@ -67,9 +67,13 @@ __device__ __forceinline__ void take_max(MinAt &a, float v, int i) {
 // Per node of the level: box, split axis and value, count of shapes going
 // right, leaf decision.  The box is reduced across the CTA over shapes
 // 1..n-1 (index-aware, so the result is the sequential one) and then merged
-// with shape 0's bound; one thread sums the midpoints in order from shared
-// memory.  node_* are the level's node arrays; out_* are indexed by the
-// node's breadth-first id.
+// with shape 0's bound.  The mean midpoint is three sequential float sums
+// (one per axis, in vector order): lane 0 of warps 0, 1 and 2 each sums one
+// axis of a staged chunk while warps 3-7 stage the next chunk into the other
+// half of a double buffer, so the sums run back to back at the adds' latency.
+// node_* are the level's node arrays; out_* are indexed by the node's
+// breadth-first id.
+constexpr int kKdStageWarps = kKdThreads / 32 - 3;
 __global__ void __launch_bounds__(kKdThreads) k_kd_fold(
     const float *__restrict__ verts, const uint8_t *__restrict__ type, const int32_t *__restrict__ ids,
     const int32_t *__restrict__ node_start, const int32_t *__restrict__ node_cnt,
@@ -77,9 +81,9 @@ __global__ void __launch_bounds__(kKdThreads) k_kd_fold(
     uint32_t *__restrict__ n_internal_elems, uint32_t *__restrict__ n_leaf_elems,
     uint32_t *__restrict__ n_children, int32_t *__restrict__ node_rc, float *__restrict__ out_box,
     int32_t *__restrict__ out_leaf) {
-    __shared__ float sm[3][kKdChunk];        // scaled midpoints
+    __shared__ float sm[2][3][kKdChunk];     // scaled midpoints, double-buffered
     __shared__ MinAt s_box[kKdThreads / 32][6];
-    __shared__ float s_split, s_box0[6];
+    __shared__ float s_split, s_box0[6], s_mid[3];
     __shared__ int s_axis;
     __shared__ uint32_t s_right[kKdThreads / 32];
     const int k = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -87,10 +91,13 @@ __global__ void __launch_bounds__(kKdThreads) k_kd_fold(
     const float recp = (float)(1.0 / (double)cnt);
     MinAt bx[6];
     for (int a = 0; a < 6; ++a) { bx[a].v = (a & 1) ? -INFINITY : INFINITY; bx[a].i = 0x7fffffff; }
-    float mid[3] = {0.f, 0.f, 0.f};
-    for (int base = 0; base < cnt; base += kKdChunk) {
-        const int m = min(kKdChunk, cnt - base);
-        for (int j = tid; j < m; j += kKdThreads) {
+    float mid = 0.f;                          // warps 0-2, lane 0: axis w
+    const int nchunks = (cnt + kKdChunk - 1) / kKdChunk;
+    const int st = tid - 3 * 32;              // staging thread index (warps 3-7)
+    auto stage = [&](int c) {
+        const int base = c * kKdChunk, m = min(kKdChunk, cnt - base);
+        float(*buf)[kKdChunk] = sm[c & 1];
+        for (int j = st; j < m; j += kKdStageWarps * 32) {
             float b[6], md[3];
             kd_shape(verts, type, ids[start + base + j], b, md);
             const int gi = base + j;
@@ -101,18 +108,22 @@ __global__ void __launch_bounds__(kKdThreads) k_kd_fold(
                 take_min(bx[2], b[2], gi); take_max(bx[3], b[3], gi);
                 take_min(bx[4], b[4], gi); take_max(bx[5], b[5], gi);
             }
-            for (int a = 0; a < 3; ++a) sm[a][j] = md[a] * recp;
+            for (int a = 0; a < 3; ++a) buf[a][j] = md[a] * recp;
         }
-        __syncthreads();
-        if (tid == 0) {                      // KDTree.cpp:127-135: shapes 1..n-1 in order
-            for (int j = base == 0 ? 1 : 0; j < m; ++j) {
-                mid[0] += sm[0][j];
-                mid[1] += sm[1][j];
-                mid[2] += sm[2][j];
-            }
+    };
+    if (st >= 0) stage(0);
+    __syncthreads();
+    for (int c = 0; c < nchunks; ++c) {
+        if (st >= 0) {
+            if (c + 1 < nchunks) stage(c + 1);
+        } else if (lane == 0) {               // KDTree.cpp:127-135: shapes 1..n-1 in order
+            const int base = c * kKdChunk, m = min(kKdChunk, cnt - base);
+            const float *v = sm[c & 1][w];
+            for (int j = base == 0 ? 1 : 0; j < m; ++j) mid += v[j];
         }
         __syncthreads();
     }
+    if (w < 3 && lane == 0) s_mid[w] = mid;
     // the box over shapes 1..n-1, then merged into shape 0's bound
     for (int o = 16; o > 0; o >>= 1) {
         for (int a = 0; a < 6; ++a) {
@@ -139,7 +150,7 @@ __global__ void __launch_bounds__(kKdThreads) k_kd_fold(
         const float xd = box[1] - box[0], yd = box[3] - box[2], zd = box[5] - box[4];
         const int axis = xd >= yd ? (xd >= zd ? 0 : 2) : (yd >= zd ? 1 : 2);   // KDTree.cpp:72-86
         s_axis = axis;
-        s_split = mid[axis];
+        s_split = s_mid[axis];
         float *ob = out_box + 6 * (size_t)node_gid[k];
         for (int a = 0; a < 6; ++a) ob[a] = box[a];
     }

@@ -217,30 +217,65 @@ __device__ __forceinline__ uint32_t morton30(uint32_t a, uint32_t b, uint32_t c)
 // reference's descending stable order.  Blocks walk the shapes from the end
 // back to the start: the tail of the array, read last by k_centroid_bounds,
 // is still in L2 when this kernel starts.
+// HIST: the digit histograms of the four radix passes are counted here as
+// well (per-CTA shared counters, flushed once per CTA), so no separate
+// histogram kernel re-reads the keys; a digit that every valid lane of the
+// warp shares (spatially coherent keys) costs one atomic.
+template <bool HIST>
 __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
                                                  const float4 *__restrict__ aabbs,
                                                  const uint8_t *__restrict__ type, int all_tri,
-                                                 int n, const BuildState *st,
+                                                 int n, BuildState *st,
                                                  uint32_t *__restrict__ keys) {
     pdl_begin();
+    __shared__ uint32_t s_hist[HIST ? 4 * 256 : 1];
+    if (HIST) {
+        for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) s_hist[i] = 0u;
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
     float lo[3], hi[3];
     for (int a = 0; a < 3; ++a) { lo[a] = ord2f(st->cmin[a]); hi[a] = ord2f(st->cmax[a]); }
     const int nblocks = (n + 255) / 256;
     for (int blk = nblocks - 1 - (int)blockIdx.x; blk >= 0; blk -= gridDim.x) {
-        int i = blk * 256 + threadIdx.x;
-        if (i >= n) continue;
-        bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
-        f3 p;
-        if (tri) {   // the triangle's centroid is its bound's centre
-            const float4 b0 = aabbs[2 * (size_t)i], b1 = aabbs[2 * (size_t)i + 1];
-            p = mk3((b0.x + b0.y) / 2.0f, (b0.z + b0.w) / 2.0f, (b1.x + b1.y) / 2.0f);
-        } else {
-            p = shape_centroid(verts, i, false);
+        const int i = blk * 256 + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0;
+        if (valid) {
+            bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
+            f3 p;
+            if (tri) {   // the triangle's centroid is its bound's centre
+                const float4 b0 = aabbs[2 * (size_t)i], b1 = aabbs[2 * (size_t)i + 1];
+                p = mk3((b0.x + b0.y) / 2.0f, (b0.z + b0.w) / 2.0f, (b1.x + b1.y) / 2.0f);
+            } else {
+                p = shape_centroid(verts, i, false);
+            }
+            uint32_t qa = quantise10(p.x, lo[0], hi[0]);
+            uint32_t qb = quantise10(p.y, lo[1], hi[1]);
+            uint32_t qc = quantise10(p.z, lo[2], hi[2]);
+            key = ~morton30(qa & 1023u, qb & 1023u, qc & 1023u);
+            keys[i] = key;
         }
-        uint32_t qa = quantise10(p.x, lo[0], hi[0]);
-        uint32_t qb = quantise10(p.y, lo[1], hi[1]);
-        uint32_t qc = quantise10(p.z, lo[2], hi[2]);
-        keys[i] = ~morton30(qa & 1023u, qb & 1023u, qc & 1023u);
+        if (HIST) {
+            const unsigned vm = __ballot_sync(0xffffffffu, valid);
+            if (vm) {                               // lane 0 is valid when any lane is
+#pragma unroll
+                for (int d = 0; d < 4; ++d) {
+                    const uint32_t dg = (key >> (8 * d)) & 255u;
+                    const uint32_t d0 = __shfl_sync(0xffffffffu, dg, 0);
+                    if (__all_sync(0xffffffffu, !valid || dg == d0)) {
+                        if (lane == 0) atomicAdd(&s_hist[d * 256 + d0], (uint32_t)__popc(vm));
+                    } else if (valid) {
+                        atomicAdd(&s_hist[d * 256 + dg], 1u);
+                    }
+                }
+            }
+        }
+    }
+    if (HIST) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x)
+            if (s_hist[i]) atomicAdd(&st->hist[0][0] + i, s_hist[i]);
     }
 }
 
@@ -1765,12 +1800,21 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
     if (e != cudaSuccess) return e;
     const int red_grid = grid_for(n, 256, sm_count * 8);
     k_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state, b.aabbs);
-    e = launch_chained(k_morton, red_grid, 256, 0, s, (const float *)b.verts, (const float4 *)b.aabbs,
-                       (const uint8_t *)b.type, all_tri, n, (const BuildState *)b.state, b.keys);
-    if (e != cudaSuccess) return e;
-    e = launch_chained(k_hist4, grid_for((n + kHistItems - 1) / kHistItems, 256, sm_count * 4), 256, 0, s,
-                       (const uint32_t *)b.keys, n, b.state);
-    if (e != cudaSuccess) return e;
+#ifndef PTGPU_MORTON_HIST
+#define PTGPU_MORTON_HIST 1
+#endif
+    if (PTGPU_MORTON_HIST) {
+        e = launch_chained(k_morton<true>, red_grid, 256, 0, s, (const float *)b.verts, (const float4 *)b.aabbs,
+                           (const uint8_t *)b.type, all_tri, n, b.state, b.keys);
+        if (e != cudaSuccess) return e;
+    } else {
+        e = launch_chained(k_morton<false>, red_grid, 256, 0, s, (const float *)b.verts, (const float4 *)b.aabbs,
+                           (const uint8_t *)b.type, all_tri, n, b.state, b.keys);
+        if (e != cudaSuccess) return e;
+        e = launch_chained(k_hist4, grid_for((n + kHistItems - 1) / kHistItems, 256, sm_count * 4), 256, 0, s,
+                           (const uint32_t *)b.keys, n, b.state);
+        if (e != cudaSuccess) return e;
+    }
     const size_t pass_words = (size_t)ntiles_sort * 256;
     const int32_t *no_seg = nullptr;
     // pass 0: keys -> (keys_alt, vals_alt); 1: alt -> tmp; 2: tmp -> alt; 3: alt -> sorted
