@@ -145,6 +145,30 @@ __global__ void k_init_state(BuildState *st) {
     }
 }
 
+// The state block, the radix passes' look-back words and the emission's
+// arrival counters of a single-tree build, cleared in one launch (block 0
+// also writes the state's initial values).
+__global__ void k_init_build(BuildState *st, uint4 *__restrict__ status, size_t status_quads,
+                             uint32_t *__restrict__ arrivals, size_t arrival_words) {
+    if (blockIdx.x == 0) {
+        const int t = threadIdx.x;
+        for (int i = t; i < 5 * 256; i += blockDim.x) (&st->hist[0][0])[i] = 0u;
+        if (t < 5) st->tile_counter[t] = 0u;
+        if (t == 0) {
+            st->error = 0u;
+            st->top_ticket = 0u;
+            for (int a = 0; a < 3; ++a) {   // the reference's FLT_MAX / FLT_MIN initial values
+                st->cmin[a] = f2ord(FLT_MAX);
+                st->cmax[a] = f2ord(FLT_MIN);
+            }
+        }
+    }
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < status_quads; i += stride) status[i] = z;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < arrival_words; i += stride) arrivals[i] = 0u;
+}
+
 // Centroid bounds, and each shape's bound stored as one aligned 32-byte
 // record for the later kernels (the emission kernel gathers it in sorted
 // order: one sector per leaf instead of a 36-byte vertex triple).
@@ -953,6 +977,11 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
                                                         ptgpu_bvh_node *__restrict__ btn,
                                                         float *__restrict__ win_bounds, int nblocks) {
     pdl_begin();
+#if PTGPU_PDL
+    // k_emit_upper (64 CTAs for 4M leaves) may launch and wait beside this
+    // persistent grid, which leaves room for it on every SM
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
     __shared__ __align__(16) uint32_t rec[kEmitLeaves * kRecWords];
     __shared__ float slot_b[8][32 * 7];     // per warp: the bounds of its 31 nodes, 7 floats apart
     __shared__ float wb[8 * 6];
@@ -1793,13 +1822,14 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
     cudaError_t e = launch_lbvh_prepare_attrs();
     if (e != cudaSuccess) return e;
     const size_t smem = sizeof(SortSmem);
-    k_init_state<<<1, 256, 0, s>>>(b.state);
-    e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(b.arrivals, 0, block_bound_count(n) * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
+    // status words: a multiple of 4 (tiles * 256 * 5), cleared as 16-byte words
+    if (reinterpret_cast<uintptr_t>(b.status) & 15) return cudaErrorInvalidValue;
+    k_init_build<<<sm_count * 2, 256, 0, s>>>(b.state, reinterpret_cast<uint4 *>(b.status),
+                                              sort_status_words(n) / 4, b.arrivals, block_bound_count(n));
     const int red_grid = grid_for(n, 256, sm_count * 8);
-    k_centroid_bounds<<<red_grid, 256, 0, s>>>(b.verts, b.type, all_tri, n, b.state, b.aabbs);
+    e = launch_chained(k_centroid_bounds, red_grid, 256, 0, s, (const float *)b.verts, (const uint8_t *)b.type,
+                       all_tri, n, b.state, b.aabbs);
+    if (e != cudaSuccess) return e;
 #ifndef PTGPU_MORTON_HIST
 #define PTGPU_MORTON_HIST 1
 #endif
