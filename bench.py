@@ -173,13 +173,19 @@ class CpuReference:
         self.acc = oracle.make_accel(abi.ACCEL_BVH, btn, btl, reference_leafness=True)
         self.seeds = oracle.make_seeds(1, 2 * W * H)
         self.threads = threads or os.cpu_count() or 1
-        # calibrate on one row of 16 pixels per thread
-        self.rows, self.cols = 1, 16 * self.threads
+        # the port spreads rows over its threads (OpenMP over rows, as DrawBox
+        # does), so a block has at least one row per thread; calibrate on
+        # 8 pixels per row
+        self.rows, self.cols = min(H, self.threads), 8
         dt = self._run()
         px_per_s = self.rows * self.cols / max(dt, 1e-6)
-        want = max(self.threads, int(px_per_s * target_s))
-        self.cols = min(W, want)
-        self.rows = max(1, min(H, want // self.cols))
+        want = max(self.rows * 8, int(px_per_s * target_s))
+        per_row = -(-want // self.rows)
+        if per_row <= W:
+            self.cols = per_row
+        else:                       # wider than the frame: more rows, a multiple of the threads
+            self.cols = W
+            self.rows = min(H, -(-(-(-want // W)) // self.threads) * self.threads)
 
     def _run(self):
         r0, c0 = H // 2 - self.rows // 2, W // 2 - self.cols // 2
@@ -196,6 +202,32 @@ class CpuReference:
                 "by the oracle, brute-force shadow rays as in IntersectP; %.1f s" %
                 (self.cols, self.rows, W, H, MAX_DEPTH, dt))
         return px / dt / 1e6, self.threads, desc
+
+    def sample_one_thread(self):
+        """The same port on one thread, over the middle row of the block."""
+        rows, cols, threads = self.rows, self.cols, self.threads
+        self.rows, self.threads = 1, 1
+        try:
+            dt = self._run()
+            return cols / dt / 1e6, "%dx1 pixel block (the middle row of the block), %.1f s" % (cols, dt)
+        finally:
+            self.rows, self.cols, self.threads = rows, cols, threads
+
+
+def cpu_model():
+    """The host CPU's name as /proc/cpuinfo gives it (model name, or the Arm
+    implementer / part codes)."""
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model"):
+        for line in info:
+            if line.startswith(key):
+                return line.split(":", 1)[1].strip()
+    impl = [l.split(":", 1)[1].strip() for l in info if l.startswith("CPU implementer")]
+    part = [l.split(":", 1)[1].strip() for l in info if l.startswith("CPU part")]
+    return "implementer %s part %s" % (impl[0] if impl else "?", part[0] if part else "?")
 
 
 def run_reference(args, rank, world, pg):
@@ -264,8 +296,16 @@ def bench_closest(ctx, torch, scenes, warmup, steps):
             ms.append(e0.elapsed_time(e1))
     hits = int(d_hit.sum().item())
     m = float(np.mean(ms))
+    # bytes-per-ray model: 24 B ray + 8 B result + 60 B per node visit + 36 B
+    # per primitive test, with visits and tests counted by the GPU (one
+    # extra, untimed pass)
+    visits, tests = ctx.trace_closest_stats_device(d_rays.data_ptr(), RAYS_N, d_t.data_ptr(), d_id.data_ptr(),
+                                                   d_hit.data_ptr())
+    model_bytes = 32 * RAYS_N + 60 * visits + 36 * tests
     return {"metric": "closest-hit Mrays/s", "rays": RAYS_N, "n_tris": LBVH_N,
-            "value": RAYS_N / m / 1e3, "unit": "Mrays/s", "ms": m, "hit_fraction": hits / RAYS_N}
+            "value": RAYS_N / m / 1e3, "unit": "Mrays/s", "ms": m, "hit_fraction": hits / RAYS_N,
+            "node_visits_per_ray": visits / RAYS_N, "prim_tests_per_ray": tests / RAYS_N,
+            "model_bytes": model_bytes}
 
 
 def bench_ingest(pt, abi, scenes, n_tris=INGEST_N, reps=3):
@@ -573,16 +613,25 @@ def main():
                           "traffic": ncu_traffic("lbvh_build_soup4m.txt", "traffic_bytes_per_build"),
                           "peak_kind": peak_kind, "model": "252 B/triangle, whole build"}
         line["lbvh"] = lb
-        line["closest_hit"] = bench_closest(lctx, torch, scenes, 1, 3)
+        ch = bench_closest(lctx, torch, scenes, 1, 3)
+        ch_ach = ch["model_bytes"] / (ch["ms"] / 1e3) / 1e9
+        ch["roofline"] = {"bound": "hbm", "achieved": ch_ach, "peak": hbm_peak, "unit": "GB/s",
+                          "frac": ch_ach / hbm_peak, "peak_kind": peak_kind, "kernel": "k_trace_closest_p",
+                          "model": "per ray 32 B + 60 B/node visit + 36 B/prim test, GPU-counted; "
+                                   "served by L1/L2 (profiles/k_trace_closest_p_soup1m_4mrays.txt)"}
+        line["closest_hit"] = ch
         lctx.close()
         line["ingest"] = bench_ingest(pt, abi, scenes)
         if not args.no_batched:
             data, specs, line["batched"] = bench_batched(pt, abi, scenes, torch)
             line["served"] = bench_served(pt, abi, data, specs)
         if rank == 0:
-            v, cores, desc = CpuReference(shapes, lc, cam, target_s=args.ref_seconds).sample()
+            cref = CpuReference(shapes, lc, cam, target_s=args.ref_seconds)
+            v, cores, desc = cref.sample()
+            v1, desc1 = cref.sample_one_thread()
             line["cpu_baseline"] = {"value": v, "unit": "Msamples/s", "cores": cores,
-                                    "kind": "port", "sample": desc}
+                                    "kind": "port", "sample": desc, "cpu": cpu_model(),
+                                    "one_thread": {"value": v1, "sample": desc1}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -218,6 +218,12 @@ int  ptgpu_trace_closest(ptgpu_ctx *ctx, const ptgpu_ray *rays, uint32_t n,
 int  ptgpu_trace_closest_device(ptgpu_ctx *ctx, const ptgpu_ray *d_rays,
                                 uint32_t n, float *d_t, uint32_t *d_id,
                                 int32_t *d_hit);
+/* ptgpu_trace_closest_device with traversal counters on, synchronised:
+ * stats[0] = node visits, stats[1] = primitive tests over all n rays (the
+ * benchmark's bytes-per-ray model; no counterpart in the reference). */
+int  ptgpu_trace_closest_stats(ptgpu_ctx *ctx, const ptgpu_ray *d_rays,
+                               uint32_t n, float *d_t, uint32_t *d_id,
+                               int32_t *d_hit, uint64_t *stats);
 int  ptgpu_get_stream(ptgpu_ctx *ctx, void **stream);
 
 /* ---- batched scenes ------------------------------------------------------- */

@@ -24,7 +24,7 @@ EXPORTS = [
     "ptgpu_make_seeds", "ptgpu_set_seeds", "ptgpu_get_seeds", "ptgpu_reset_accumulation",
     "ptgpu_draw_frame", "ptgpu_render_async", "ptgpu_synchronize", "ptgpu_get_colors",
     "ptgpu_get_pixels", "ptgpu_get_current_sample", "ptgpu_trace_closest",
-    "ptgpu_trace_closest_device", "ptgpu_get_stream", "ptgpu_render_stats",
+    "ptgpu_trace_closest_device", "ptgpu_trace_closest_stats", "ptgpu_get_stream", "ptgpu_render_stats",
     "ptgpu_build_bvh_noalloc",
     "ptgpu_batch_create", "ptgpu_batch_destroy", "ptgpu_batch_add", "ptgpu_batch_build",
     "ptgpu_batch_tune", "ptgpu_batch_render", "ptgpu_batch_reset", "ptgpu_batch_get_pixels",
@@ -106,6 +106,7 @@ def lib():
         L.ptgpu_get_current_sample.argtypes = [vp, ctypes.POINTER(i32)]
         L.ptgpu_trace_closest.argtypes = [vp, vp, u32, vp, vp, vp]
         L.ptgpu_trace_closest_device.argtypes = [vp, vp, u32, vp, vp, vp]
+        L.ptgpu_trace_closest_stats.argtypes = [vp, vp, u32, vp, vp, vp, vp]
         L.ptgpu_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
         L.ptgpu_render_stats.argtypes = [vp, u32, vp]
         _lib = L
@@ -305,6 +306,13 @@ class Context:
         _check(lib().ptgpu_trace_closest_device(self._h, ctypes.c_void_p(d_rays), n,
                                                 ctypes.c_void_p(d_t), ctypes.c_void_p(d_id),
                                                 ctypes.c_void_p(d_hit)))
+
+    def trace_closest_stats_device(self, d_rays, n, d_t, d_id, d_hit):
+        """trace_closest_device with counters: (node visits, primitive tests)."""
+        st = np.zeros(2, np.uint64)
+        _check(lib().ptgpu_trace_closest_stats(self._h, ctypes.c_void_p(d_rays), n, ctypes.c_void_p(d_t),
+                                               ctypes.c_void_p(d_id), ctypes.c_void_p(d_hit), _p(st)))
+        return int(st[0]), int(st[1])
 
     def stream(self):
         s = ctypes.c_void_p()

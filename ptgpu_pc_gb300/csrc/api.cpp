@@ -780,6 +780,24 @@ int ptgpu_trace_closest_device(ptgpu_ctx *c, const ptgpu_ray *d_rays, uint32_t n
     return PTGPU_OK;
 }
 
+int ptgpu_trace_closest_stats(ptgpu_ctx *c, const ptgpu_ray *d_rays, uint32_t n, float *d_t,
+                              uint32_t *d_id, int32_t *d_hit, uint64_t *stats) {
+    if (!c || !stats || (n && (!d_rays || !d_t || !d_id || !d_hit))) return fail(PTGPU_E_INVAL, "null argument");
+    if (c->accel_built < 0) return fail(PTGPU_E_STATE, "build an acceleration structure first");
+    cudaSetDevice(c->device);
+    unsigned long long *d = nullptr;
+    CK(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess)
+        e = launch_trace_closest(make_view(c), d_rays, (int)n, d_t, d_id, d_hit, c->stream,
+                                 c->d_pixctr.as<unsigned int>() + 1, d);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(stats, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "closest-hit counters");
+    return PTGPU_OK;
+}
+
 int ptgpu_trace_closest(ptgpu_ctx *c, const ptgpu_ray *rays, uint32_t n, float *t, uint32_t *id,
                         int32_t *hit) {
     if (!c || (n && (!rays || !t || !id || !hit))) return fail(PTGPU_E_INVAL, "null argument");

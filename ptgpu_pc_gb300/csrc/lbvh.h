@@ -174,9 +174,10 @@ size_t wf_carve_bytes(int paths, int n_lights);
 void wf_carve(WfArgs &a, void *base, int paths, int n_lights);
 cudaError_t launch_wavefront(WfArgs a, int iterations, int grid, cudaStream_t s);
 // counter: a device word for the persistent kernel (null: one thread per ray)
+// stats (with counter): node visits and primitive tests added to stats[0..1]
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
                                  uint32_t *id, int32_t *hit, cudaStream_t s,
-                                 unsigned int *counter = nullptr);
+                                 unsigned int *counter = nullptr, unsigned long long *stats = nullptr);
 
 // kd_gpu.cu: the KD tree of KDTree::build on the device, from the build
 // vertices and types; node ids breadth-first (scratch kept between builds)

@@ -584,14 +584,17 @@ cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int g
 // writes their results and refills them together -- the render kernel's
 // schedule without the shading.  Each ray visits its nodes in the same order
 // as in trace_query.
-template <bool WIDE>
+// COUNT: node visits and primitive tests summed into stats[0..1].
+template <bool WIDE, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_closest_p(TraceView tv,
                                                           const ptgpu_ray *__restrict__ rays,
                                                           int n, float *__restrict__ tout,
                                                           uint32_t *__restrict__ idout,
                                                           int32_t *__restrict__ hitout,
-                                                          unsigned int *counter, int refill) {
+                                                          unsigned int *counter, int refill,
+                                                          unsigned long long *stats) {
     const int lane = threadIdx.x & 31;
+    Counts cnt = {0, 0};
     const TraceRoot root = view_root(tv);
     Trav q;
     q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0; q.skip = -1;
@@ -615,7 +618,7 @@ __global__ void __launch_bounds__(128) k_trace_closest_p(TraceView tv,
                     const float *rp = reinterpret_cast<const float *>(rays + ray);
                     const f3 o = mk3(rp[0], rp[1], rp[2]);
                     const f3 d = mk3(rp[3], rp[4], rp[5]);
-                    if (trav_begin<false>(tv, root, q, o, d, false, 0.f, nullptr)) fin = true;
+                    if (trav_begin<COUNT>(tv, root, q, o, d, false, 0.f, COUNT ? &cnt : nullptr)) fin = true;
                     else trav = true;
                 }
             }
@@ -626,7 +629,7 @@ __global__ void __launch_bounds__(128) k_trace_closest_p(TraceView tv,
             if (!busy) break;
             const unsigned live = __ballot_sync(0xffffffffu, !done);
             if (__popc(live & ~busy) * 32 >= refill * __popc(live)) break;
-            if (trav && trav_step<WIDE, false>(tv, q, stack, nullptr)) {
+            if (trav && trav_step<WIDE, COUNT>(tv, q, stack, COUNT ? &cnt : nullptr)) {
                 trav = false;
                 fin = true;
             }
@@ -638,10 +641,15 @@ __global__ void __launch_bounds__(128) k_trace_closest_p(TraceView tv,
             hitout[ray] = q.hit;
         }
     }
+    if (COUNT) {
+        atomicAdd(stats + 0, (unsigned long long)cnt.v);
+        atomicAdd(stats + 1, (unsigned long long)cnt.p);
+    }
 }
 
 cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int n, float *t,
-                                 uint32_t *id, int32_t *hit, cudaStream_t s, unsigned int *counter) {
+                                 uint32_t *id, int32_t *hit, cudaStream_t s, unsigned int *counter,
+                                 unsigned long long *stats) {
     if (n <= 0) return cudaSuccess;
     if (!counter) {   // one thread per ray
         if (tv.nodes4) k_trace_closest<true><<<(n + 127) / 128, 128, 0, s>>>(tv, rays, n, t, id, hit);
@@ -650,14 +658,19 @@ cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int
     }
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    const void *k = tv.nodes4 ? (const void *)k_trace_closest_p<true> : (const void *)k_trace_closest_p<false>;
+    const void *k = tv.nodes4 ? (const void *)k_trace_closest_p<true, false>
+                              : (const void *)k_trace_closest_p<false, false>;
     int grid = resident_grid(k, 128, 0);
     const int need = (n + 127) / 128;
     if (grid <= 0 || grid > need) grid = need;
-    if (tv.nodes4)
-        k_trace_closest_p<true><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, PTGPU_RENDER_REFILL);
-    else
-        k_trace_closest_p<false><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, PTGPU_RENDER_REFILL);
+    const int r = PTGPU_RENDER_REFILL;
+    if (stats) {
+        if (tv.nodes4) k_trace_closest_p<true, true><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, r, stats);
+        else k_trace_closest_p<false, true><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, r, stats);
+    } else {
+        if (tv.nodes4) k_trace_closest_p<true, false><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, r, nullptr);
+        else k_trace_closest_p<false, false><<<grid, 128, 0, s>>>(tv, rays, n, t, id, hit, counter, r, nullptr);
+    }
     return cudaGetLastError();
 }
 
