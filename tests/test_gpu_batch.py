@@ -20,6 +20,10 @@ def _scene_set():
     out.append((sh, lc, cam, 32, 24, 4))
     sh, lc, cam = scenes.icosphere_scene(level=6, seed=9, n_tris=20000)
     out.append((sh, lc, cam, 24, 32, 1))
+    # tiny trees: 2 shapes (no treelet round applies) and 3
+    near = scenes.camera([0.5, 0.5, 3.0])
+    out.append((scenes.triangle_soup(2, seed=31), 0, near, 16, 16, 2))
+    out.append((scenes.triangle_soup(3, seed=32), 0, near, 16, 8, 3))
     return out
 
 
