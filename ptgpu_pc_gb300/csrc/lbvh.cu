@@ -189,14 +189,37 @@ __device__ __forceinline__ void centroid_shape(const float *__restrict__ v, bool
     }
 }
 
+// A warp takes 32 consecutive shapes per step: their 1152 bytes of vertices
+// arrive as 72 coalesced 16-byte loads (vertex array on a 16-byte boundary),
+// go through shared memory, and each lane reads back its own 9 floats
+// (stride 9: no bank conflicts).  The tail, or an unaligned array, takes one
+// shape per lane directly.
 __global__ void __launch_bounds__(256) k_centroid_bounds(const float *__restrict__ verts,
                                                           const uint8_t *__restrict__ type,
                                                           int all_tri, int n, BuildState *st,
                                                           float4 *__restrict__ aabbs) {
     pdl_begin();
+    __shared__ __align__(16) float s_v[256 / 32][32 * 9];
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        centroid_shape(verts + 9 * (size_t)i, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i, lo, hi);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool aligned = (reinterpret_cast<uintptr_t>(verts) & 15) == 0;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    float *sv = s_v[w];
+    for (int base = (blockIdx.x * (blockDim.x >> 5) + w) * 32; base < n; base += nwarps * 32) {
+        const int i = base + lane;
+        if (aligned && base + 32 <= n) {
+            const float4 *src = reinterpret_cast<const float4 *>(verts + 9 * (size_t)base);
+            float4 *dst = reinterpret_cast<float4 *>(sv);
+            dst[lane] = __ldg(src + lane);
+            dst[lane + 32] = __ldg(src + lane + 32);
+            if (lane < 8) dst[lane + 64] = __ldg(src + lane + 64);
+            __syncwarp();
+            centroid_shape(sv + 9 * lane, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i, lo, hi);
+            __syncwarp();
+        } else if (i < n) {
+            centroid_shape(verts + 9 * (size_t)i, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i, lo, hi);
+        }
+    }
     for (int a = 0; a < 3; ++a) {
         for (int o = 16; o > 0; o >>= 1) {
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
@@ -204,8 +227,7 @@ __global__ void __launch_bounds__(256) k_centroid_bounds(const float *__restrict
         }
     }
     __shared__ float s_lo[8][3], s_hi[8][3];
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) for (int a = 0; a < 3; ++a) { s_lo[w][a] = lo[a]; s_hi[w][a] = hi[a]; }
+    if (lane == 0) for (int a = 0; a < 3; ++a) { s_lo[w][a] = lo[a]; s_hi[w][a] = hi[a]; }
     __syncthreads();
     if (threadIdx.x < 3) {
         int a = threadIdx.x;
