@@ -247,16 +247,20 @@ __device__ __forceinline__ uint32_t quantise10(float p, float lo, float hi) {
     return __float2uint_rz(q);
 }
 
-__device__ __forceinline__ uint32_t morton30(uint32_t a, uint32_t b, uint32_t c) {
+// bit j of a 10-bit value to bit 3j, by shift-and-mask steps that spread
+// the bits apart (the same result as moving each bit separately)
+__host__ __device__ __forceinline__ uint32_t spread3(uint32_t x) {
+    x &= 1023u;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__host__ __device__ __forceinline__ uint32_t morton30(uint32_t a, uint32_t b, uint32_t c) {
     // bit j of a (j = 9..0) goes to 3j+2, of b to 3j+1, of c to 3j (CLBVH.cpp:158-163)
-    uint32_t code = 0;
-#pragma unroll
-    for (int j = 0; j < 10; ++j) {
-        code |= ((a >> j) & 1u) << (3 * j + 2);
-        code |= ((b >> j) & 1u) << (3 * j + 1);
-        code |= ((c >> j) & 1u) << (3 * j + 0);
-    }
-    return code;
+    return (spread3(a) << 2) | (spread3(b) << 1) | spread3(c);
 }
 
 // Morton keys.  The sort key is ~code, so an ascending stable sort gives the
