@@ -65,7 +65,7 @@ enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 // of its live lanes wait without a query in flight (32: when every query of
 // the warp is answered).
 #ifndef PTGPU_RENDER_REFILL
-#define PTGPU_RENDER_REFILL 20
+#define PTGPU_RENDER_REFILL 22
 #endif
 // traversal steps between two looks at the warp's waiting lanes
 #ifndef PTGPU_RENDER_STEPS
