@@ -7,6 +7,8 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -84,8 +86,12 @@ struct ptgpu_ctx {
     int block = 128;
     int flags = 0;
     // scene
-    std::vector<ptgpu_shape> h_shapes;   // empty after ptgpu_stream_scene (device copy only)
+    // the scene's shape records: d_shapes holds them as set (never modified);
+    // the host copy is made from it only when a call needs one
+    std::vector<ptgpu_shape> h_shapes;
     bool host_shapes = false;            // h_shapes holds the scene
+    DevBuf d_export;                     // the records with a BVH build's index / morton / b
+    bool export_ready = false;           // d_export holds them
     bool kd_indexed = false;             // a KD build numbered the host copy's shapes
     IngestScratch ingest;
     uint32_t n = 0, light_cnt = 0;
@@ -233,7 +239,7 @@ int ptgpu_destroy(ptgpu_ctx *c) {
                       &c->d_tcount, &c->d_tcost, &c->d_aabbs,
                       &c->d_nodes, &c->d_nodes4, &c->d_prims, &c->d_prim_id, &c->d_root_box, &c->d_identity,
                       &c->d_colors, &c->d_pixels, &c->d_seeds, &c->d_err, &c->d_pixctr, &c->d_wf, &c->d_rays, &c->d_t,
-                      &c->d_cost, &c->d_order, &c->d_order_scr,
+                      &c->d_cost, &c->d_order, &c->d_order_scr, &c->d_export,
                       &c->d_id, &c->d_hit};
     for (DevBuf *b : bufs) b->release();
     c->ingest.release();
@@ -282,12 +288,13 @@ static int finish_scene(ptgpu_ctx *c, uint32_t n, uint32_t light_cnt, int n_ligh
     c->bvh_valid = false;
     c->kd_valid = false;
     c->shapes_exported = false;
+    c->export_ready = false;
     c->kd_indexed = false;
     c->current_sample = 0;
     return PTGPU_OK;
 }
 
-int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt) {
+static int ptgpu_set_shapes_body(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt) {
     if (!c || (!shapes && n)) return fail(PTGPU_E_INVAL, "null argument");
     if (n == 0) return fail(PTGPU_E_INVAL, "a scene needs at least one shape");
     if (n >= (1u << 30)) return fail(PTGPU_E_INVAL, "too many shapes (limit 2^30-1)");
@@ -295,8 +302,9 @@ int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32
         if (shapes[i].type != PTGPU_SPHERE && shapes[i].type != PTGPU_TRIANGLE)
             return fail(PTGPU_E_INVAL, "shape " + std::to_string(i) + " has an unknown type");
     cudaSetDevice(c->device);
-    c->h_shapes.assign(shapes, shapes + n);
-    c->host_shapes = true;
+    c->h_shapes.clear();
+    c->h_shapes.shrink_to_fit();
+    c->host_shapes = false;
     bool all_tri = true;
     for (uint32_t i = 0; i < n; ++i) if (shapes[i].type != PTGPU_TRIANGLE) { all_tri = false; break; }
     // emitters visited by SampleLights: the first light_cnt in index order
@@ -310,22 +318,17 @@ int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32
     return finish_scene(c, n, light_cnt, (int)lights.size(), all_tri);
 }
 
-// The host copy of the scene, for the calls that need one after
-// ptgpu_stream_scene: the device records with the fields a BVH build exports
-// (index, morton_code, b) as the host copy would hold them -- the loader's
-// zeros, or the index a KD build gives.
+// The host copy of the scene, for the calls that need one (ptgpu_get_shapes
+// without a BVH, the host KD build): the records as set, copied from the
+// device once, with the numbering a KD build gives them.
 static int ensure_host_shapes(ptgpu_ctx *c) {
     if (c->host_shapes) return PTGPU_OK;
     c->h_shapes.resize(c->n);
     CK(cudaMemcpyAsync(c->h_shapes.data(), c->d_shapes.p, (size_t)c->n * sizeof(ptgpu_shape),
                        cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    for (uint32_t i = 0; i < c->n; ++i) {
-        ptgpu_shape &s = c->h_shapes[i];
-        s.index = c->kd_indexed ? (int32_t)i : 0;
-        s.morton_code = 0;
-        std::memset(&s.b, 0, sizeof(s.b));
-    }
+    if (c->kd_indexed)
+        for (uint32_t i = 0; i < c->n; ++i) { c->h_shapes[i].index = (int32_t)i; c->h_shapes[i].morton_code = 0; }
     c->host_shapes = true;
     return PTGPU_OK;
 }
@@ -337,17 +340,21 @@ int ptgpu_get_shape_count(ptgpu_ctx *c, uint32_t *n, uint32_t *light_cnt) {
     return PTGPU_OK;
 }
 
-int ptgpu_get_shapes(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
+static int ptgpu_get_shapes_body(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
     if (!c || !out) return fail(PTGPU_E_INVAL, "null argument");
     if (n != c->n) return fail(PTGPU_E_INVAL, "shape count mismatch");
     if (c->accel_built == PTGPU_ACCEL_BVH && c->bvh_valid && c->d_keys.p) {
         cudaSetDevice(c->device);
         if (!c->shapes_exported) {
-            CK(launch_export_shapes(c->d_shapes.as<ptgpu_shape>(), c->d_verts.as<float>(),
-                                    c->d_type.as<uint8_t>(), c->d_keys.as<uint32_t>(), (int)n, c->stream));
+            CK(c->d_export.ensure((size_t)n * sizeof(ptgpu_shape)));
+            CK(launch_export_shapes(c->d_shapes.as<ptgpu_shape>(), c->d_export.as<ptgpu_shape>(),
+                                    c->d_verts.as<float>(), c->d_type.as<uint8_t>(), c->d_keys.as<uint32_t>(),
+                                    (int)n, c->stream));
             c->shapes_exported = true;
+            c->export_ready = true;
         }
-        CK(cudaMemcpyAsync(out, c->d_shapes.p, (size_t)n * sizeof(ptgpu_shape), cudaMemcpyDeviceToHost, c->stream));
+        const void *src = c->export_ready ? c->d_export.p : c->d_shapes.p;
+        CK(cudaMemcpyAsync(out, src, (size_t)n * sizeof(ptgpu_shape), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         return PTGPU_OK;
     }
@@ -357,7 +364,7 @@ int ptgpu_get_shapes(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
     return PTGPU_OK;
 }
 
-int ptgpu_read_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
+static int ptgpu_read_scene_body(ptgpu_ctx *c, const char *path, int32_t *walllight) {
     if (!c || !path) return fail(PTGPU_E_INVAL, "null argument");
     LoadedScene sc;
     std::string err;
@@ -370,7 +377,7 @@ int ptgpu_read_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
     return ptgpu_set_camera(c, &sc.camera);
 }
 
-int ptgpu_stream_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
+static int ptgpu_stream_scene_body(ptgpu_ctx *c, const char *path, int32_t *walllight) {
     if (!c || !path) return fail(PTGPU_E_INVAL, "null argument");
     CompactScene sc;
     std::string err;
@@ -453,7 +460,7 @@ static int prepare_bvh_trace(ptgpu_ctx *c) {
     return prepare_wide(c);
 }
 
-int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
+static int ptgpu_build_body(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
     if (!c) return fail(PTGPU_E_INVAL, "null context");
     if (c->n == 0) return fail(PTGPU_E_STATE, "no shapes set");
     if (accel < 0 || accel > 2) return fail(PTGPU_E_INVAL, "accel must be 0, 1 or 2");
@@ -819,3 +826,54 @@ int ptgpu_trace_closest(ptgpu_ctx *c, const ptgpu_ray *rays, uint32_t n, float *
 }
 
 }  // extern "C"
+
+// C entry points: no C++ exception crosses the C ABI
+int ptgpu_set_shapes(ptgpu_ctx *c, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt) {
+    try {
+        return ptgpu_set_shapes_body(c, shapes, n, light_cnt);
+    } catch (const std::bad_alloc &) {
+        return fail(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return fail(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_get_shapes(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
+    try {
+        return ptgpu_get_shapes_body(c, out, n);
+    } catch (const std::bad_alloc &) {
+        return fail(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return fail(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_read_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
+    try {
+        return ptgpu_read_scene_body(c, path, walllight);
+    } catch (const std::bad_alloc &) {
+        return fail(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return fail(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_stream_scene(ptgpu_ctx *c, const char *path, int32_t *walllight) {
+    try {
+        return ptgpu_stream_scene_body(c, path, walllight);
+    } catch (const std::bad_alloc &) {
+        return fail(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return fail(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_build(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
+    try {
+        return ptgpu_build_body(c, accel, flags);
+    } catch (const std::bad_alloc &) {
+        return fail(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return fail(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}

@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -179,7 +181,7 @@ int ptgpu_batch_destroy(ptgpu_batch *b) {
     return PTGPU_OK;
 }
 
-int ptgpu_batch_add(ptgpu_batch *b, const ptgpu_scene *sc, int32_t *scene_id) {
+static int ptgpu_batch_add_body(ptgpu_batch *b, const ptgpu_scene *sc, int32_t *scene_id) {
     if (!b || !sc || !sc->shapes || !sc->seeds) return record_error(PTGPU_E_INVAL, "null argument");
     if ((int)b->scenes.size() >= kMaxSegments)
         return record_error(PTGPU_E_RANGE, "a batch holds at most 256 scenes");
@@ -209,7 +211,7 @@ int ptgpu_batch_add(ptgpu_batch *b, const ptgpu_scene *sc, int32_t *scene_id) {
     return PTGPU_OK;
 }
 
-int ptgpu_batch_build(ptgpu_batch *b, uint32_t flags) {
+static int ptgpu_batch_build_body(ptgpu_batch *b, uint32_t flags) {
     if (!b) return record_error(PTGPU_E_INVAL, "null batch");
     if (b->scenes.empty()) return record_error(PTGPU_E_STATE, "no scenes added");
     if (flags & PTGPU_FLAG_MORTON_DELTA) return record_error(PTGPU_E_INVAL, "build flag not supported");
@@ -543,3 +545,24 @@ int ptgpu_batch_info_get(ptgpu_batch *b, ptgpu_batch_info *info) {
 }
 
 }  // extern "C"
+
+// C entry points: no C++ exception crosses the C ABI
+int ptgpu_batch_add(ptgpu_batch *b, const ptgpu_scene *sc, int32_t *scene_id) {
+    try {
+        return ptgpu_batch_add_body(b, sc, scene_id);
+    } catch (const std::bad_alloc &) {
+        return record_error(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return record_error(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_batch_build(ptgpu_batch *b, uint32_t flags) {
+    try {
+        return ptgpu_batch_build_body(b, flags);
+    } catch (const std::bad_alloc &) {
+        return record_error(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return record_error(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}

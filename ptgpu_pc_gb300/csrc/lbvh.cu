@@ -1756,18 +1756,20 @@ __global__ void k_gather_prims(const int32_t *__restrict__ order, int count,
 }
 
 // Shape.b / index / morton_code as CLBVH::CLBVH leaves them in the shapes
-__global__ void k_export_shapes(ptgpu_shape *__restrict__ shapes, const float *__restrict__ verts,
-                                const uint8_t *__restrict__ type, const uint32_t *__restrict__ keys,
-                                int n) {
+__global__ void k_export_shapes(const ptgpu_shape *__restrict__ shapes, ptgpu_shape *__restrict__ out,
+                                const float *__restrict__ verts, const uint8_t *__restrict__ type,
+                                const uint32_t *__restrict__ keys, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float b[6];
     shape_bound(verts, i, type[i] == PTGPU_TRIANGLE, b);
-    shapes[i].index = i;
-    shapes[i].morton_code = ~keys[i];
-    shapes[i].b.min_x = b[0]; shapes[i].b.max_x = b[1];
-    shapes[i].b.min_y = b[2]; shapes[i].b.max_y = b[3];
-    shapes[i].b.min_z = b[4]; shapes[i].b.max_z = b[5];
+    ptgpu_shape s = shapes[i];
+    s.index = i;
+    s.morton_code = ~keys[i];
+    s.b.min_x = b[0]; s.b.max_x = b[1];
+    s.b.min_y = b[2]; s.b.max_y = b[3];
+    s.b.min_z = b[4]; s.b.max_z = b[5];
+    out[i] = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -1961,10 +1963,10 @@ cudaError_t launch_gather_prims(const int32_t *order, int count, const float4 *p
     return cudaGetLastError();
 }
 
-cudaError_t launch_export_shapes(ptgpu_shape *shapes, const float *verts, const uint8_t *type,
-                                 const uint32_t *keys, int n, cudaStream_t s) {
+cudaError_t launch_export_shapes(const ptgpu_shape *shapes, ptgpu_shape *out, const float *verts,
+                                 const uint8_t *type, const uint32_t *keys, int n, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_export_shapes<<<(n + 255) / 256, 256, 0, s>>>(shapes, verts, type, keys, n);
+    k_export_shapes<<<(n + 255) / 256, 256, 0, s>>>(shapes, out, verts, type, keys, n);
     return cudaGetLastError();
 }
 

@@ -194,11 +194,22 @@ bool read_obj(const char *path, Obj &obj, std::string &err, int threads) {
         runs.push_back(r);
         start = stop;
     }
+    // runs on their own threads; a run whose thread cannot be started is
+    // done on this one (no exception leaves the reader)
     auto for_runs = [&](auto fn) {
         std::vector<std::thread> th;
-        for (size_t k = 1; k < runs.size(); ++k) th.emplace_back([&, k] { fn(runs[k]); });
+        std::vector<char> started(runs.size(), 0);
+        for (size_t k = 1; k < runs.size(); ++k) {
+            try {
+                th.emplace_back([&, k] { fn(runs[k]); });
+                started[k] = 1;
+            } catch (...) {
+            }
+        }
         if (!runs.empty()) fn(runs[0]);
         for (auto &x : th) x.join();
+        for (size_t k = 1; k < runs.size(); ++k)
+            if (!started[k]) fn(runs[k]);
     };
     for_runs([&](ObjRun &r) { obj_count(buf, end_idx, r); });
     int64_t nv = 0, nt = 0;

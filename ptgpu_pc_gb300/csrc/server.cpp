@@ -27,6 +27,8 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -645,7 +647,7 @@ int ptgpu_server_destroy(ptgpu_server *s) {
     return PTGPU_OK;
 }
 
-int ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
+static int ptgpu_server_add_scene_body(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
                            uint32_t build_flags, int32_t *scene) {
     if (!s || !shapes) return record_error(PTGPU_E_INVAL, "null argument");
     if (n < 2) return record_error(PTGPU_E_INVAL, "a served scene needs at least 2 shapes");
@@ -667,7 +669,7 @@ int ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t 
     return PTGPU_OK;
 }
 
-int ptgpu_server_add_scene_file(ptgpu_server *s, const char *path, uint32_t build_flags, int32_t *scene) {
+static int ptgpu_server_add_scene_file_body(ptgpu_server *s, const char *path, uint32_t build_flags, int32_t *scene) {
     if (!s || !path) return record_error(PTGPU_E_INVAL, "null argument");
     if (build_flags & PTGPU_FLAG_MORTON_DELTA) return record_error(PTGPU_E_INVAL, "build flag not supported");
     // read once to check the file and count its shapes and lights; the
@@ -692,7 +694,7 @@ int ptgpu_server_add_scene_file(ptgpu_server *s, const char *path, uint32_t buil
     return PTGPU_OK;
 }
 
-int ptgpu_server_submit(ptgpu_server *s, const ptgpu_request *r, int64_t *ticket) {
+static int ptgpu_server_submit_body(ptgpu_server *s, const ptgpu_request *r, int64_t *ticket) {
     if (!s || !r || !ticket) return record_error(PTGPU_E_INVAL, "null argument");
     if (r->width <= 0 || r->height <= 0 || (int64_t)r->width * r->height > (1ll << 28))
         return record_error(PTGPU_E_INVAL, "bad image size");
@@ -762,3 +764,35 @@ int ptgpu_server_info_get(ptgpu_server *s, ptgpu_server_info *info) {
 }
 
 }  // extern "C"
+
+// C entry points: no C++ exception crosses the C ABI
+int ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
+                           uint32_t build_flags, int32_t *scene) {
+    try {
+        return ptgpu_server_add_scene_body(s, shapes, n, light_cnt, build_flags, scene);
+    } catch (const std::bad_alloc &) {
+        return record_error(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return record_error(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_server_add_scene_file(ptgpu_server *s, const char *path, uint32_t build_flags, int32_t *scene) {
+    try {
+        return ptgpu_server_add_scene_file_body(s, path, build_flags, scene);
+    } catch (const std::bad_alloc &) {
+        return record_error(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return record_error(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
+
+int ptgpu_server_submit(ptgpu_server *s, const ptgpu_request *r, int64_t *ticket) {
+    try {
+        return ptgpu_server_submit_body(s, r, ticket);
+    } catch (const std::bad_alloc &) {
+        return record_error(PTGPU_E_OOM, "out of host memory");
+    } catch (const std::exception &e) {
+        return record_error(PTGPU_E_INVAL, std::string("unexpected error: ") + e.what());
+    }
+}
