@@ -84,6 +84,7 @@ def run_batch(a):
             b.add(sh, lc, cam, sp["res"], sp["res"], sp["spp"], pt.make_seeds(sp["seed"], 2 * sp["res"] ** 2),
                   max_depth=6)
         b.build(abi.FLAG_TREELET | abi.treelet_sweeps(2))
+        print("batch build %.2f ms (device)" % b.info()["build_ms"])
         for i in range(a.frames):
             t0 = time.perf_counter()
             b.reset()
