@@ -1476,27 +1476,26 @@ __device__ void treelet_warp(int root, float root_cost, ptgpu_bvh_node *btn, ptg
 // arrival at a node owns it.  The lanes of a warp that own a node in the same
 // round hand their treelets to the whole warp one after another.
 constexpr int kTreeletThreads = 128;
-// leaves a warp climbs from (its other lanes only help in the treelets):
-// fewer leaves per warp put more warps, and so more treelets, in flight
-// (82k-shape scene, LBVH + 2 rounds: 32 -> 1.29 ms, 16 -> 1.22, 8 -> 1.33)
-#ifndef PTGPU_TREELET_LPW
-#define PTGPU_TREELET_LPW 16
-#endif
-constexpr int kTreeletLpw = PTGPU_TREELET_LPW;
-__device__ __forceinline__ int treelet_leaf(int lane) {
-    return lane < kTreeletLpw ? (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kTreeletLpw + lane
-                              : 0x7fffffff;
+// Leaves a warp climbs from (its other lanes only help in the treelets):
+// fewer leaves per warp put more warps, and so more treelets, in flight,
+// which pays on small trees (82k-shape scene, LBVH + 2 rounds: 32 -> 1.29 ms,
+// 16 -> 1.22 ms) and costs on large ones, where 32 already fill the GPU
+// (17.3M leaves of a batch: build 97 ms with 16 against 81 ms with 32).
+__device__ __forceinline__ int treelet_leaf(int lane, int lpw) {
+    return lane < lpw ? (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * lpw + lane : 0x7fffffff;
 }
-__host__ __device__ constexpr int treelet_grid(int leaves) {
-    return (int)(((int64_t)leaves + kTreeletLpw * (kTreeletThreads / 32) - 1) / (kTreeletLpw * (kTreeletThreads / 32)));
+static int treelet_lpw(int64_t leaves) { return leaves < (1 << 20) ? 16 : 32; }
+static int treelet_grid(int64_t leaves, int lpw) {
+    return (int)((leaves + (int64_t)lpw * (kTreeletThreads / 32) - 1) / ((int64_t)lpw * (kTreeletThreads / 32)));
 }
+
 __global__ void __launch_bounds__(kTreeletThreads) k_treelet(ptgpu_bvh_node *btn,
                                                               ptgpu_bvh_node *btl, int n,
-                                                              int *counters, float *cost) {
+                                                              int *counters, float *cost, int lpw) {
     __shared__ TreeletSmem s_tl[kTreeletThreads / 32];
     TreeletSmem &sm = s_tl[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
-    const int k = treelet_leaf(lane);
+    const int k = treelet_leaf(lane, lpw);
     int node = k < n ? btl[k].nParent : -1;
     bool active = node >= 0 && node < n - 1;
     while (__any_sync(0xffffffffu, active)) {
@@ -1589,11 +1588,12 @@ __global__ void k_treelet_finish_seg(ptgpu_bvh_node *btn, const int32_t *__restr
 
 __global__ void __launch_bounds__(kTreeletThreads) k_treelet_seg(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl,
                                                                   const int32_t *__restrict__ seg_off, int n_segs,
-                                                                  int n_total, int *counters, float *cost) {
+                                                                  int n_total, int *counters, float *cost,
+                                                                  int lpw) {
     __shared__ TreeletSmem s_tl[kTreeletThreads / 32];
     TreeletSmem &sm = s_tl[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
-    const int k = treelet_leaf(lane);
+    const int k = treelet_leaf(lane, lpw);
     int g = 0, off = 0, n = 0;
     if (k < n_total) {
         g = (int)segment_of(seg_off, n_segs, k);
@@ -1652,8 +1652,8 @@ cudaError_t launch_treelet_seg(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, const i
     k_treelet_prepare_seg<<<(n_internal + 255) / 256, 256, 0, s>>>(btn, seg_off, n_segs, n_internal, counters);
     for (int it = 0; it < sweeps; ++it) {
         if (it > 0) cudaMemsetAsync(counters, 0, sizeof(int) * (size_t)n_internal, s);
-        k_treelet_seg<<<treelet_grid(n_total), kTreeletThreads, 0, s>>>(
-            btn, btl, seg_off, n_segs, n_total, counters, cost);
+        k_treelet_seg<<<treelet_grid(n_total, treelet_lpw(n_total)), kTreeletThreads, 0, s>>>(
+            btn, btl, seg_off, n_segs, n_total, counters, cost, treelet_lpw(n_total));
     }
     k_treelet_finish_seg<<<(n_internal + 255) / 256, 256, 0, s>>>(btn, seg_off, n_segs, n_internal, cost);
     return cudaGetLastError();
@@ -1665,8 +1665,8 @@ cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int 
     k_treelet_prepare<<<(n + 255) / 256, 256, 0, s>>>(btn, n, counters);
     for (int it = 0; it < sweeps; ++it) {
         if (it > 0) cudaMemsetAsync(counters, 0, sizeof(int) * (size_t)(n - 1), s);
-        k_treelet<<<treelet_grid(n), kTreeletThreads, 0, s>>>(
-            btn, btl, n, counters, cost);
+        k_treelet<<<treelet_grid(n, treelet_lpw(n)), kTreeletThreads, 0, s>>>(
+            btn, btl, n, counters, cost, treelet_lpw(n));
     }
     k_treelet_finish<<<(n + 255) / 256, 256, 0, s>>>(btn, n, cost);
     return cudaGetLastError();
