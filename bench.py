@@ -283,6 +283,49 @@ def bench_lbvh(pt, abi, scenes, torch, warmup, steps):
                  "unit": "Mtris/s", "ms": ms, "min_ms": float(np.min(times)), "builds": steps}
 
 
+def sah_cost(btn, btl):
+    """SAH cost of a BVHNodeGPU tree (Karras & Aila 2013: Ci = 1.2 per internal
+    node, Ct = 1.0 per leaf, areas relative to the root's)."""
+    def area(b):                 # b: min_x, max_x, min_y, max_y, min_z, max_z per row
+        b = b.astype(np.float64)
+        dx, dy, dz = b[:, 1] - b[:, 0], b[:, 3] - b[:, 2], b[:, 5] - b[:, 4]
+        return 2.0 * (dx * dy + dy * dz + dz * dx)
+    a_in, a_lf = area(btn["bound"]), area(btl["bound"])
+    return float((1.2 * a_in.sum() + 1.0 * a_lf.sum()) / a_in[0])
+
+
+def bench_treelet(pt, abi, shapes, lc, cam, torch, rounds=(0, 1, 2), frames=4):
+    """Treelet reoptimisation report on the benchmark scene: SAH cost of the
+    tree and frame time (CUDA events, after a warm-up frame) for 0, 1 and 2
+    rounds, and the build time each costs."""
+    out = {"rounds": [], "sah": [], "frame_ms": [], "build_ms": []}
+    for r in rounds:
+        flags = (abi.FLAG_TREELET | abi.treelet_sweeps(r)) if r else 0
+        with pt.Context(W, H, accel=abi.ACCEL_BVH, max_depth=MAX_DEPTH) as ctx:
+            ctx.set_shapes(shapes, lc)
+            ctx.build(abi.ACCEL_BVH, flags)
+            build_ms = ctx.last_build_ms()
+            btn, btl = ctx.get_bvh()
+            ctx.set_camera(cam)
+            ctx.set_seeds(pt.make_seeds(1, 2 * W * H))
+            stream = torch.cuda.ExternalStream(ctx.stream())
+            ms = []
+            for f in range(frames + 1):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ctx.reset()
+                e0.record(stream)
+                ctx.render_async(SPP)
+                e1.record(stream)
+                e1.synchronize()
+                if f > 0:
+                    ms.append(e0.elapsed_time(e1))
+        out["rounds"].append(r)
+        out["sah"].append(sah_cost(btn, btl))
+        out["frame_ms"].append(float(np.mean(ms)))
+        out["build_ms"].append(build_ms)
+    return out
+
+
 def bench_closest(ctx, torch, scenes, warmup, steps):
     rays = scenes.random_rays(RAYS_N, seed=4)
     d_rays = torch.from_numpy(rays.view(np.uint8).reshape(-1)).cuda()
@@ -626,6 +669,7 @@ def main():
                           "traffic": ncu_traffic("lbvh_build_soup4m.txt", "traffic_bytes_per_build"),
                           "peak_kind": peak_kind, "model": "252 B/triangle, whole build"}
         line["lbvh"] = lb
+        line["treelet"] = bench_treelet(pt, abi, shapes, lc, cam, torch)
         ch = bench_closest(lctx, torch, scenes, 1, 3)
         ch_ach = ch["model_bytes"] / (ch["ms"] / 1e3) / 1e9
         ch["roofline"] = {"bound": "hbm", "achieved": ch_ach, "peak": hbm_peak, "unit": "GB/s",
