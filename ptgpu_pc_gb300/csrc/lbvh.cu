@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(256) k_seg_morton(const float *__restrict__ ve
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 #ifndef PTGPU_SORT_ITEMS
-#define PTGPU_SORT_ITEMS 15
+#define PTGPU_SORT_ITEMS 20
 #endif
 constexpr int kSortItems = PTGPU_SORT_ITEMS;
 constexpr int kSortTile = kSortThreads * kSortItems;
@@ -508,6 +508,9 @@ constexpr int kSpinLimit = 1 << 22;
 #define PTGPU_LOOKBACK 8
 #endif
 constexpr int kLookback = PTGPU_LOOKBACK;   // predecessors read per look-back step
+#ifndef PTGPU_SORT_PREFETCH
+#define PTGPU_SORT_PREFETCH 1
+#endif
 #ifndef PTGPU_SORT_MINBLOCKS
 #define PTGPU_SORT_MINBLOCKS 3
 #endif
@@ -548,6 +551,52 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_t
     uint32_t warp_base = w ? s_tmp[w - 1] : 0u;
     __syncthreads();
     return warp_base + x - v;
+}
+
+// Decoupled look-back of one digit (one thread per digit): publishes the
+// tile's count as an aggregate (tile 0: as inclusive), sums predecessors back
+// to the first inclusive word and publishes the inclusive count.  Returns the
+// count of this digit in all earlier tiles; a wait past kSpinLimit sets the
+// build's error bit and the tile's abort flag.
+__device__ __forceinline__ uint32_t lookback_digit(uint32_t *status, int tile, int tid, uint32_t count,
+                                                   BuildState *st, int &abort_flag) {
+    uint32_t *my = status + (size_t)tile * 256 + tid;
+    uint32_t excl = 0;
+    if (tile == 0) {
+        st_volatile(my, kFlagInc | count);
+        return 0u;
+    }
+    st_volatile(my, kFlagAgg | count);
+    // the words of kLookback predecessors are read at once, then summed from
+    // the nearest back to the first inclusive one; a word not yet published
+    // ends the window and is read again
+    int p = tile - 1;
+    bool timed_out = false;
+    int spins = 0;
+    while (p >= 0) {
+        uint32_t v[kLookback];
+#pragma unroll
+        for (int q = 0; q < kLookback; ++q)
+            v[q] = p - q >= 0 ? ld_volatile(status + (size_t)(p - q) * 256 + tid) : 0u;
+        int q = 0;
+        bool done = false;
+#pragma unroll
+        for (; q < kLookback; ++q) {
+            const uint32_t f = v[q] & (3u << 30);
+            if (f == 0u) break;
+            excl += v[q] & kValMask;
+            if (f == kFlagInc) { done = true; break; }
+        }
+        if (done) break;
+        p -= q;
+        if (q < kLookback) {
+            if (++spins > kSpinLimit) { timed_out = true; break; }
+            __nanosleep(32);
+        }
+    }
+    if (timed_out) { atomicOr(&st->error, 1u); abort_flag = 1; }
+    st_volatile(my, kFlagInc | ((excl + count) & kValMask));
+    return excl;
 }
 
 struct SortSmem {
@@ -597,14 +646,20 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     for (int i = tid; i < 2 * kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.u.match[0][0][0])[i] = zero4;
     // global digit offsets for this pass
     uint32_t gcount = st->hist[pass][tid];
+#if PTGPU_SORT_PREFETCH
+    __syncthreads();                          // the tile id, seg_off, the cleared arrays
+    uint32_t goff = 0;
+#else
     uint32_t goff = block_excl_scan256(gcount, sm.scan_tmp);
     __syncthreads();
+#endif
     const int tile = sm.tile;
     // 64-bit positions: measured faster here than 32-bit ones (4M keys: 4 passes
     // 0.148 -> 0.183 ms with int)
     const int64_t base = (int64_t)tile * kSortTile;
+    // the values are read again when they are staged (from L2), so that the
+    // registers they would hold go to more items per tile
     uint32_t key[kSortItems];
-    int32_t val[kSortItems];
     uint32_t rank[kSortItems];
     const unsigned lt_mask = (1u << lane) - 1u;
     // all loads first: the ranking below synchronises the warp per item, and
@@ -613,14 +668,17 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     for (int j = 0; j < kSortItems; ++j) {
         const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
         const bool valid = idx < n;
-        val[j] = valid ? (FIRST ? (int32_t)idx : vals_in[idx]) : -1;
-        if (!SEG) key[j] = valid ? keys_in[idx] : 0xffffffffu;
+        if constexpr (SEG) {   // seg_off is in shared memory after the barrier above
+            const int32_t v = valid ? vals_in[idx] : -1;
+            key[j] = v >= 0 ? segment_of(sm.seg_off, n_segs, v) : 0xffffffffu;
+        } else {
+            key[j] = valid ? keys_in[idx] : 0xffffffffu;
+        }
     }
-    if (SEG) {   // seg_off is in shared memory after the barrier above
-#pragma unroll
-        for (int j = 0; j < kSortItems; ++j)
-            key[j] = val[j] >= 0 ? segment_of(sm.seg_off, n_segs, val[j]) : 0xffffffffu;
-    }
+#if PTGPU_SORT_PREFETCH
+    // the scan of the global digit counts runs while the tile's loads are in flight
+    goff = block_excl_scan256(gcount, sm.scan_tmp);
+#endif
 #pragma unroll
     for (int j = 0; j < kSortItems; ++j) {
         const int idx = base + w * 32 * kSortItems + j * 32 + lane;
@@ -655,43 +713,7 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     }
     uint32_t dstart = block_excl_scan256(count, sm.scan_tmp);
     sm.digit_start[tid] = dstart;
-    // decoupled look-back, one digit per thread
-    uint32_t *my = status + (size_t)tile * 256 + tid;
-    uint32_t excl = 0;
-    if (tile == 0) {
-        st_volatile(my, kFlagInc | count);
-    } else {
-        st_volatile(my, kFlagAgg | count);
-        // the words of kLookback predecessors are read at once, then summed
-        // from the nearest back to the first inclusive one; a word not yet
-        // published ends the window and is read again
-        int p = tile - 1;
-        bool timed_out = false;
-        int spins = 0;
-        while (p >= 0) {
-            uint32_t v[kLookback];
-#pragma unroll
-            for (int q = 0; q < kLookback; ++q)
-                v[q] = p - q >= 0 ? ld_volatile(status + (size_t)(p - q) * 256 + tid) : 0u;
-            int q = 0;
-            bool done = false;
-#pragma unroll
-            for (; q < kLookback; ++q) {
-                const uint32_t f = v[q] & (3u << 30);
-                if (f == 0u) break;
-                excl += v[q] & kValMask;
-                if (f == kFlagInc) { done = true; break; }
-            }
-            if (done) break;
-            p -= q;
-            if (q < kLookback) {
-                if (++spins > kSpinLimit) { timed_out = true; break; }
-                __nanosleep(32);
-            }
-        }
-        if (timed_out) { atomicOr(&st->error, 1u); sm.abort = 1; }
-        st_volatile(my, kFlagInc | ((excl + count) & kValMask));
-    }
+    const uint32_t excl = lookback_digit(status, tile, tid, count, st, sm.abort);
     sm.tile_excl[tid] = goff + excl - dstart;       // + tile position = destination (mod 2^32)
     __syncthreads();
     // scatter into shared memory in tile-sorted order
@@ -701,7 +723,8 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
             uint32_t dig = (key[j] >> shift) & 255u;
             uint32_t pos = sm.digit_start[dig] + sm.warp_hist[w][dig] + rank[j];
             sm.u.st.keys[pos] = key[j];
-            sm.u.st.vals[pos] = val[j];
+            const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
+            sm.u.st.vals[pos] = FIRST ? (int32_t)idx : vals_in[idx];
         }
     }
     __syncthreads();
