@@ -189,6 +189,18 @@ __device__ __forceinline__ void centroid_shape(const float *__restrict__ v, bool
     }
 }
 
+#ifndef PTGPU_CENTROID_PIPE
+#define PTGPU_CENTROID_PIPE 1
+#endif
+// 16-byte global -> shared copies that complete asynchronously (L2 only)
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // A warp takes 32 consecutive shapes per step: their 1152 bytes of vertices
 // arrive as 72 coalesced 16-byte loads (vertex array on a 16-byte boundary),
 // go through shared memory, and each lane reads back its own 9 floats
@@ -199,11 +211,43 @@ __global__ void __launch_bounds__(256) k_centroid_bounds(const float *__restrict
                                                           int all_tri, int n, BuildState *st,
                                                           float4 *__restrict__ aabbs) {
     pdl_begin();
-    __shared__ __align__(16) float s_v[256 / 32][32 * 9];
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const bool aligned = (reinterpret_cast<uintptr_t>(verts) & 15) == 0;
     const int nwarps = gridDim.x * (blockDim.x >> 5);
+#if PTGPU_CENTROID_PIPE
+    // two buffers per warp: the next 32 shapes' vertices are copied in
+    // (cp.async, 16 bytes per copy) while the current ones are bounded
+    __shared__ __align__(16) float s_v[256 / 32][2][32 * 9];
+    const int stride = nwarps * 32;
+    auto fetch = [&](int b, int slot) {
+        if (aligned && b + 32 <= n) {
+            const float4 *src = reinterpret_cast<const float4 *>(verts + 9 * (size_t)b);
+            float4 *dst = reinterpret_cast<float4 *>(s_v[w][slot]);
+            cp_async16(dst + lane, src + lane);
+            cp_async16(dst + lane + 32, src + lane + 32);
+            if (lane < 8) cp_async16(dst + lane + 64, src + lane + 64);
+        }
+        cp_async_commit();                        // one group per step, empty or not
+    };
+    int base = (blockIdx.x * (blockDim.x >> 5) + w) * 32;
+    fetch(base, 0);
+    for (int it = 0; base < n; ++it, base += stride) {
+        fetch(base + stride, (it + 1) & 1);
+        cp_async_wait1();                         // this step's copies have landed
+        __syncwarp();
+        const int i = base + lane;
+        if (aligned && base + 32 <= n) {
+            centroid_shape(s_v[w][it & 1] + 9 * lane, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i,
+                           lo, hi);
+        } else if (i < n) {
+            centroid_shape(verts + 9 * (size_t)i, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i, lo, hi);
+        }
+        __syncwarp();                             // the buffer is read before it is refilled
+    }
+    cp_async_wait0();
+#else
+    __shared__ __align__(16) float s_v[256 / 32][32 * 9];
     float *sv = s_v[w];
     for (int base = (blockIdx.x * (blockDim.x >> 5) + w) * 32; base < n; base += nwarps * 32) {
         const int i = base + lane;
@@ -220,6 +264,7 @@ __global__ void __launch_bounds__(256) k_centroid_bounds(const float *__restrict
             centroid_shape(verts + 9 * (size_t)i, all_tri || type[i] == PTGPU_TRIANGLE, aabbs + 2 * (size_t)i, lo, hi);
         }
     }
+#endif
     for (int a = 0; a < 3; ++a) {
         for (int o = 16; o > 0; o >>= 1) {
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
@@ -266,7 +311,8 @@ __host__ __device__ __forceinline__ uint32_t morton30(uint32_t a, uint32_t b, ui
 // Morton keys.  The sort key is ~code, so an ascending stable sort gives the
 // reference's descending stable order.  Blocks walk the shapes from the end
 // back to the start: the tail of the array, read last by k_centroid_bounds,
-// is still in L2 when this kernel starts.
+// is still in L2 when this kernel starts.  Each thread loads its next step's
+// record before it makes the current key.
 // HIST: the digit histograms of the four radix passes are counted here as
 // well (per-CTA shared counters, flushed once per CTA), so no separate
 // histogram kernel re-reads the keys; a digit that every valid lane of the
@@ -287,19 +333,39 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
     float lo[3], hi[3];
     for (int a = 0; a < 3; ++a) { lo[a] = ord2f(st->cmin[a]); hi[a] = ord2f(st->cmax[a]); }
     const int nblocks = (n + 255) / 256;
+    // the next step's records are loaded before this step's keys are made
+    // (a triangle's bound record; a sphere's centre in r0.xyz)
+    auto fetch = [&](int blk, float4 &r0, float4 &r1, bool &tri) {
+        const int i = blk * 256 + threadIdx.x;
+        r0 = r1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        tri = true;
+        if (blk >= 0 && i < n) {
+            tri = all_tri || type[i] == PTGPU_TRIANGLE;
+            if (tri) {
+                r0 = aabbs[2 * (size_t)i];
+                r1 = aabbs[2 * (size_t)i + 1];
+            } else {
+                const f3 c = shape_centroid(verts, i, false);
+                r0 = make_float4(c.x, c.y, c.z, 0.f);
+            }
+        }
+    };
+    float4 c0, c1;
+    bool ctri;
+    fetch(nblocks - 1 - (int)blockIdx.x, c0, c1, ctri);
     for (int blk = nblocks - 1 - (int)blockIdx.x; blk >= 0; blk -= gridDim.x) {
+        float4 n0, n1;
+        bool ntri;
+        fetch(blk - (int)gridDim.x, n0, n1, ntri);
         const int i = blk * 256 + threadIdx.x;
         const bool valid = i < n;
         uint32_t key = 0;
         if (valid) {
-            bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
             f3 p;
-            if (tri) {   // the triangle's centroid is its bound's centre
-                const float4 b0 = aabbs[2 * (size_t)i], b1 = aabbs[2 * (size_t)i + 1];
-                p = mk3((b0.x + b0.y) / 2.0f, (b0.z + b0.w) / 2.0f, (b1.x + b1.y) / 2.0f);
-            } else {
-                p = shape_centroid(verts, i, false);
-            }
+            if (ctri)    // the triangle's centroid is its bound's centre
+                p = mk3((c0.x + c0.y) / 2.0f, (c0.z + c0.w) / 2.0f, (c1.x + c1.y) / 2.0f);
+            else
+                p = mk3(c0.x, c0.y, c0.z);
             uint32_t qa = quantise10(p.x, lo[0], hi[0]);
             uint32_t qb = quantise10(p.y, lo[1], hi[1]);
             uint32_t qc = quantise10(p.z, lo[2], hi[2]);
@@ -321,6 +387,9 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
                 }
             }
         }
+        c0 = n0;
+        c1 = n1;
+        ctri = ntri;
     }
     if (HIST) {
         __syncthreads();
@@ -495,7 +564,11 @@ __global__ void __launch_bounds__(256) k_seg_morton(const float *__restrict__ ve
 // ---------------------------------------------------------------------------
 // onesweep radix pass
 // ---------------------------------------------------------------------------
-constexpr int kSortThreads = 256;
+#ifndef PTGPU_SORT_THREADS
+#define PTGPU_SORT_THREADS 256
+#endif
+constexpr int kSortThreads = PTGPU_SORT_THREADS;   // 256 or 512; threads 0-255 own one digit each
+static_assert(kSortThreads == 256 || kSortThreads == 512, "one digit per thread of the first 256");
 constexpr int kSortWarps = kSortThreads / 32;
 #ifndef PTGPU_SORT_ITEMS
 #define PTGPU_SORT_ITEMS 20
@@ -645,7 +718,8 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     for (int i = tid; i < kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.warp_hist[0][0])[i] = zero4;
     for (int i = tid; i < 2 * kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.u.match[0][0][0])[i] = zero4;
     // global digit offsets for this pass
-    uint32_t gcount = st->hist[pass][tid];
+    const bool dig_thread = kSortThreads == 256 || tid < 256;
+    uint32_t gcount = dig_thread ? st->hist[pass][tid] : 0u;
 #if PTGPU_SORT_PREFETCH
     __syncthreads();                          // the tile id, seg_off, the cleared arrays
     uint32_t goff = 0;
@@ -707,14 +781,18 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     uint32_t count = 0;
 #pragma unroll
     for (int k = 0; k < kSortWarps; ++k) {
-        uint32_t c = sm.warp_hist[k][tid];
-        sm.warp_hist[k][tid] = count;
-        count += c;
+        if (dig_thread) {
+            uint32_t c = sm.warp_hist[k][tid];
+            sm.warp_hist[k][tid] = count;
+            count += c;
+        }
     }
     uint32_t dstart = block_excl_scan256(count, sm.scan_tmp);
-    sm.digit_start[tid] = dstart;
-    const uint32_t excl = lookback_digit(status, tile, tid, count, st, sm.abort);
-    sm.tile_excl[tid] = goff + excl - dstart;       // + tile position = destination (mod 2^32)
+    if (dig_thread) {
+        sm.digit_start[tid] = dstart;
+        const uint32_t excl = lookback_digit(status, tile, tid, count, st, sm.abort);
+        sm.tile_excl[tid] = goff + excl - dstart;   // + tile position = destination (mod 2^32)
+    }
     __syncthreads();
     // scatter into shared memory in tile-sorted order
 #pragma unroll

@@ -61,6 +61,20 @@ def test_lbvh_negative_coordinates(built_lib, orc):
     _compare(s, orc)
 
 
+def test_lbvh_mixed_spheres_triangles(built_lib, orc):
+    # spheres shuffled among triangles: whole warps of 32 shapes take both
+    # the sphere and the triangle bound and centroid forms
+    rng = np.random.default_rng(21)
+    m = 6000
+    sph = abi.spheres(rng.uniform(0.001, 0.02, m), rng.random((m, 3)), np.zeros((m, 3)),
+                      np.full((m, 3), 0.5), np.zeros(m, np.int32))
+    tri = scenes.triangle_soup(14001, seed=21)
+    s = np.zeros(len(tri) + m, abi.SHAPE)
+    s[:len(tri)] = tri
+    s[len(tri):] = sph
+    _compare(s[rng.permutation(len(s))], orc)
+
+
 @pytest.mark.parametrize("n", [1 << 20, (1 << 20) + 7])
 def test_lbvh_1m(n, built_lib, orc):
     _compare(scenes.triangle_soup(n, seed=5), orc)
