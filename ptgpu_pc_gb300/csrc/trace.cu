@@ -58,8 +58,11 @@ __device__ __forceinline__ uint32_t to_int(float x) {
 
 enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 
+#ifndef PTGPU_RENDER_SMEM_STATE
+#define PTGPU_RENDER_SMEM_STATE 1   // 72 -> 64 registers, 8 CTAs per SM: 28.73 -> 28.58 ms per frame
+#endif
 #ifndef PTGPU_RENDER_MINBLOCKS
-#define PTGPU_RENDER_MINBLOCKS 7   // 72 registers: 7 CTAs of 128 lanes per SM
+#define PTGPU_RENDER_MINBLOCKS 7   // at least 7 CTAs of 128 lanes per SM (8 at 64 registers)
 #endif
 // A warp leaves its traversal steps to shade when at least this many 32nds
 // of its live lanes wait without a query in flight (32: when every query of
@@ -102,8 +105,20 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     uint32_t t_pix = 0;  // SM clock when the lane took its pixel
     int sc = 0;          // BATCH: the lane's scene (hand-out order)
     uint32_t s0 = 0, s1 = 0;
+#if PTGPU_RENDER_SMEM_STATE
+    // the lane's colour and hit state lives in shared memory (12-byte
+    // stride: lane i on bank 3i mod 32, no conflicts): it is touched when a
+    // query is made or consumed, not while the traversal steps, and its 21
+    // registers would otherwise be held through every step
+    __shared__ f3 s_lane[7][128];
+    f3 &col = s_lane[0][threadIdx.x], &rad = s_lane[1][threadIdx.x], &tp = s_lane[2][threadIdx.x];
+    f3 &hp = s_lane[3][threadIdx.x], &nl = s_lane[4][threadIdx.x], &ld = s_lane[5][threadIdx.x];
+    f3 &pend = s_lane[6][threadIdx.x];
+    col = mk3(0.f, 0.f, 0.f); rad = col; tp = col; hp = col; nl = col; ld = col; pend = col;
+#else
     f3 col = mk3(0.f, 0.f, 0.f), rad = col, tp = col, hp = col, nl = col;
     f3 ld = col, pend = col;
+#endif
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
     q.any = 0; q.hit = 0; q.skip = -1;
