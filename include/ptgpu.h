@@ -113,7 +113,8 @@ typedef struct {
 
 /* build / render flags */
 #define PTGPU_FLAG_WAVEFRONT     0x1  /* render with the queue-based wavefront  */
-#define PTGPU_FLAG_MORTON_DELTA  0x2  /* Karras split on Morton keys (quality)  */
+#define PTGPU_FLAG_MORTON_DELTA  0x2  /* reserved (a Karras split on the Morton
+                                         keys); ptgpu_build answers E_INVAL     */
 #define PTGPU_FLAG_TREELET       0x4  /* treelet reoptimisation after refit     */
 #define PTGPU_FLAG_WIDE_TRAVERSAL 0x10 /* traverse 4-wide nodes collapsed from
                                          the 2-wide ones (default: 2-wide)      */

@@ -465,7 +465,7 @@ static int ptgpu_build_body(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
     if (c->n == 0) return fail(PTGPU_E_STATE, "no shapes set");
     if (accel < 0 || accel > 2) return fail(PTGPU_E_INVAL, "accel must be 0, 1 or 2");
     if (flags & PTGPU_FLAG_MORTON_DELTA)
-        return fail(PTGPU_E_INVAL, "build flag not supported by this build");
+        return fail(PTGPU_E_INVAL, "PTGPU_FLAG_MORTON_DELTA is reserved: the build keeps the index-prefix topology");
     if ((flags & PTGPU_FLAG_TREELET) && accel != PTGPU_ACCEL_BVH)
         return fail(PTGPU_E_INVAL, "treelet restructuring applies to the BVH only");
     cudaSetDevice(c->device);
