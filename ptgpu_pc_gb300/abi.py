@@ -100,7 +100,7 @@ SERVER_INFO = np.dtype({
 OK, E_INVAL, E_OOM, E_DEVICE, E_TIMEOUT, E_IO, E_RANGE, E_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 
 FLAG_WAVEFRONT = 0x1
-FLAG_MORTON_DELTA = 0x2
+FLAG_MORTON_DELTA = 0x2        # reserved: ptgpu_build answers E_INVAL
 FLAG_TREELET = 0x4
 FLAG_ARGS_RTL = 0x8
 FLAG_WIDE_TRAVERSAL = 0x10
