@@ -601,12 +601,14 @@ cudaError_t launch_render_batch(const RenderArgs &a, int block, int stack, int g
 // as in trace_query.
 // COUNT: node visits and primitive tests summed into stats[0..1].
 template <bool WIDE, bool COUNT>
-// 12 resident CTAs of 128 lanes per SM (40 registers, 8 bytes spilled)
-// instead of 10 at 47: 2^24 random rays against 4M triangles 24.5 -> 20.6 ms
+// Binary nodes: 12 resident CTAs of 128 lanes per SM (40 registers, 8 bytes
+// spilled) instead of 10 at 47: 2^24 random rays against 4M triangles
+// 24.5 -> 20.6 ms.  The 4-wide traversal keeps its own register count (at 12
+// CTAs it would spill 126 bytes; not measured).
 #ifndef PTGPU_CLOSEST_MINBLOCKS
 #define PTGPU_CLOSEST_MINBLOCKS 12
 #endif
-__global__ void __launch_bounds__(128, PTGPU_CLOSEST_MINBLOCKS) k_trace_closest_p(TraceView tv,
+__global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_trace_closest_p(TraceView tv,
                                                           const ptgpu_ray *__restrict__ rays,
                                                           int n, float *__restrict__ tout,
                                                           uint32_t *__restrict__ idout,
