@@ -14,7 +14,8 @@ LIB = os.path.join(HERE, "libptgpu.so")
 
 CU_SOURCES = ["lbvh.cu", "trace.cu", "wavefront.cu", "noalloc.cu", "batch.cu", "kd_gpu.cu", "ingest.cu"]
 CPP_SOURCES = ["api.cpp", "kdtree.cpp", "loader.cpp", "batch.cpp", "server.cpp"]
-HEADERS = ["device.cuh", "types.h", "lbvh.h", "lbvh_topo.cuh", "host.h", "devbuf.h", "ingest.h"]
+HEADERS = ["device.cuh", "types.h", "lbvh.h", "lbvh_topo.cuh", "host.h", "devbuf.h", "ingest.h",
+           "range_alloc.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no contraction, so float results round like the reference's

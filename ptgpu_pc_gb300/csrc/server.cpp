@@ -40,6 +40,7 @@
 #include "host.h"
 #include "ingest.h"
 #include "lbvh.h"
+#include "range_alloc.h"
 
 using namespace ptgpu;
 
@@ -50,47 +51,6 @@ using Clock = std::chrono::steady_clock;
 double ms_since(Clock::time_point t0, Clock::time_point t1) {
     return std::chrono::duration<double, std::milli>(t1 - t0).count();
 }
-
-// First-fit allocator over [0, capacity) in element units.
-struct RangeAlloc {
-    std::map<int64_t, int64_t> free_;   // start -> length
-    int64_t capacity = 0;
-    int64_t used = 0;
-    bool alloc(int64_t n, int64_t *start) {
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < n) continue;
-            *start = it->first;
-            const int64_t rest = it->second - n, s = it->first + n;
-            free_.erase(it);
-            if (rest > 0) free_[s] = rest;
-            used += n;
-            return true;
-        }
-        return false;
-    }
-    void release(int64_t start, int64_t n) {
-        used -= n;
-        auto it = free_.emplace(start, n).first;
-        auto nx = std::next(it);
-        if (nx != free_.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free_.erase(nx);
-        }
-        if (it != free_.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-    void grow(int64_t new_cap) {   // the new tail becomes free
-        if (new_cap <= capacity) return;
-        used += new_cap - capacity;   // release() below takes it off again
-        release(capacity, new_cap - capacity);
-        capacity = new_cap;
-    }
-};
 
 // A device array that grows by copying its old contents (indices stay valid).
 struct Arena {

@@ -1,5 +1,6 @@
 // host_shim.cpp -- test-only C entry points over the library's host code
-// (KD-tree build, scene loader, camera, closed-form LBVH topology), compiled
+// (KD-tree build, scene loader, camera, closed-form LBVH topology, the
+// server's slot allocator), compiled
 // without CUDA by the CPU tests.
 #include <algorithm>
 #include <cstdint>
@@ -12,6 +13,7 @@
 #define __forceinline__ inline
 #include "../../ptgpu_pc_gb300/csrc/lbvh_topo.cuh"
 #include "../../ptgpu_pc_gb300/csrc/host.h"
+#include "../../ptgpu_pc_gb300/csrc/range_alloc.h"
 
 extern "C" {
 
@@ -126,5 +128,24 @@ void shim_compact_get(ptgpu_shape *out) {
 void shim_update_camera(ptgpu_camera *cam) { ptgpu::update_camera(cam); }
 
 void shim_make_seeds(uint64_t m, uint32_t *s, uint32_t n) { ptgpu::make_seeds(m, s, n); }
+
+// the server's first-fit slot allocator
+void *shim_ra_new() { return new ptgpu::RangeAlloc(); }
+void shim_ra_delete(void *a) { delete static_cast<ptgpu::RangeAlloc *>(a); }
+void shim_ra_grow(void *a, int64_t cap) { static_cast<ptgpu::RangeAlloc *>(a)->grow(cap); }
+int shim_ra_alloc(void *a, int64_t n, int64_t *start) {
+    return static_cast<ptgpu::RangeAlloc *>(a)->alloc(n, start) ? 1 : 0;
+}
+void shim_ra_release(void *a, int64_t start, int64_t n) { static_cast<ptgpu::RangeAlloc *>(a)->release(start, n); }
+int64_t shim_ra_used(void *a) { return static_cast<ptgpu::RangeAlloc *>(a)->used; }
+// the free ranges in address order as (start, length) pairs; returns their count
+int shim_ra_free(void *a, int64_t *out, int max_pairs) {
+    int k = 0;
+    for (const auto &r : static_cast<ptgpu::RangeAlloc *>(a)->free_) {
+        if (k < max_pairs) { out[2 * k] = r.first; out[2 * k + 1] = r.second; }
+        ++k;
+    }
+    return k;
+}
 
 }

@@ -33,6 +33,14 @@ def shim(tmp_path_factory):
     L.shim_scene_get.argtypes = [vp, vp]
     L.shim_update_camera.argtypes = [vp]
     L.shim_read_obj.argtypes = [ctypes.c_char_p, ctypes.c_int, vp, vp, ctypes.c_char_p, ctypes.c_int]
+    L.shim_ra_new.restype = vp
+    L.shim_ra_delete.argtypes = [vp]
+    L.shim_ra_grow.argtypes = [vp, ctypes.c_int64]
+    L.shim_ra_alloc.argtypes = [vp, ctypes.c_int64, vp]
+    L.shim_ra_release.argtypes = [vp, ctypes.c_int64, ctypes.c_int64]
+    L.shim_ra_used.argtypes = [vp]
+    L.shim_ra_used.restype = ctypes.c_int64
+    L.shim_ra_free.argtypes = [vp, vp, ctypes.c_int]
     L.shim_obj_get.argtypes = [vp, vp]
     L.shim_read_scene_compact.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp]
     L.shim_compact_get.argtypes = [vp]
@@ -270,3 +278,60 @@ def test_compact_scene_expands_to_read_scene(shim, tmp_path):
     got = np.zeros(n2.value, abi.SHAPE)
     shim.shim_compact_get(_p(got))
     assert got.tobytes() == ref.tobytes()
+
+
+def _free_runs(busy):
+    """(start, length) of the free runs of a boolean occupancy array."""
+    runs, i, n = [], 0, len(busy)
+    while i < n:
+        if busy[i]:
+            i += 1
+            continue
+        j = i
+        while j < n and not busy[j]:
+            j += 1
+        runs.append((i, j - i))
+        i = j
+    return runs
+
+
+def test_server_slot_allocator_first_fit(shim):
+    """The server's slot allocator (range_alloc.h) against a first-fit model
+    over an occupancy array: random grows, allocations and releases give the
+    same starts, refusals, used count and (merged) free ranges."""
+    rng = np.random.default_rng(17)
+    a = shim.shim_ra_new()
+    try:
+        busy = np.zeros(0, bool)
+        live = []
+        start = ctypes.c_int64()
+        out = np.zeros(2 * 4096, np.int64)
+        for step in range(3000):
+            op = rng.random()
+            if op < 0.05 or len(busy) == 0:
+                cap = len(busy) + int(rng.integers(1, 300))
+                shim.shim_ra_grow(a, cap)
+                busy = np.concatenate([busy, np.zeros(cap - len(busy), bool)])
+            elif op < 0.6:
+                n = int(rng.integers(1, 64))
+                runs = [r for r in _free_runs(busy) if r[1] >= n]
+                ok = shim.shim_ra_alloc(a, n, ctypes.byref(start))
+                assert ok == (1 if runs else 0)
+                if runs:
+                    assert start.value == runs[0][0]
+                    busy[start.value:start.value + n] = True
+                    live.append((start.value, n))
+            elif live:
+                s, n = live.pop(int(rng.integers(len(live))))
+                shim.shim_ra_release(a, s, n)
+                busy[s:s + n] = False
+            assert shim.shim_ra_used(a) == int(busy.sum())
+            k = shim.shim_ra_free(a, out.ctypes.data, 4096)
+            assert [tuple(x) for x in out[:2 * k].reshape(-1, 2)] == _free_runs(busy)
+        # releasing everything leaves one range over the whole capacity
+        for s, n in live:
+            shim.shim_ra_release(a, s, n)
+        k = shim.shim_ra_free(a, out.ctypes.data, 4096)
+        assert k == 1 and tuple(out[:2]) == (0, len(busy)) and shim.shim_ra_used(a) == 0
+    finally:
+        shim.shim_ra_delete(a)
