@@ -97,6 +97,18 @@ typedef struct {
     int16_t min, max;             /* [min,max) into the kn index list       */
 } ptgpu_kd_node;
 
+/* The same KD tree with 32-bit fields, for trees the int16 heap above cannot
+ * express (KDNodeGPU overflows past 32,767 heap slots; an 82k-shape scene needs
+ * 2^18).  Nodes breadth-first, root at index 0, children at nLeft/nRight and
+ * the parent at nParent (-1 where there is none); a leaf owns [min, max) of the
+ * kn index list, which is the heap export's kn. */
+typedef struct {
+    int32_t leaf;                 /* 1 leaf, 0 internal                     */
+    int32_t nLeft, nRight, nParent;
+    ptgpu_bound bound;
+    int32_t min, max;
+} ptgpu_kd_node_wide;
+
 /* ---- context -------------------------------------------------------------- */
 typedef struct ptgpu_ctx ptgpu_ctx;
 
@@ -176,9 +188,24 @@ int  ptgpu_get_bvh(ptgpu_ctx *ctx, ptgpu_bvh_node *btn, ptgpu_bvh_node *btl);
  * get *kng_cnt / *kn_cnt.  PTGPU_E_RANGE if the heap overflows int16. */
 int  ptgpu_get_kdtree(ptgpu_ctx *ctx, ptgpu_kd_node *kng, int32_t *kng_cnt,
                       int32_t *kn, int32_t *kn_cnt);
+/* KDTree::getTrees (KDTree.cpp:257-270) without the int16 limit: the tree as
+ * ptgpu_kd_node_wide records (breadth-first, the heap's node order with its
+ * empty slots left out) and the same kn list.  Size query: pass NULL buffers
+ * to get *node_cnt / *kn_cnt; E_INVAL when a buffer is smaller than that. */
+int  ptgpu_get_kdtree_wide(ptgpu_ctx *ctx, ptgpu_kd_node_wide *nodes, int32_t *node_cnt,
+                           int32_t *kn, int32_t *kn_cnt);
 /* Installs caller-built BVH arrays (the ReInit upload, smallptGPU.cpp:1145-1148). */
 int  ptgpu_set_bvh(ptgpu_ctx *ctx, const ptgpu_bvh_node *btn,
                    const ptgpu_bvh_node *btl, uint32_t n);
+/* No counterpart in the reference (its look-back-free host sort never
+ * waits).  The radix sort's decoupled look-back waits for earlier tiles; a
+ * tile that has polled `polls` times (about 32 ns apart) without an answer
+ * gives up and ptgpu_build returns PTGPU_E_TIMEOUT, leaving the context
+ * usable.  The default is PTGPU_WAIT_LIMIT_DEFAULT; 0 gives up at the first
+ * wait, so any build of more than one sort tile (5,120 shapes) times out --
+ * a way to exercise the error path without a fault. */
+#define PTGPU_WAIT_LIMIT_DEFAULT 4194304u
+int  ptgpu_set_wait_limit(ptgpu_ctx *ctx, uint32_t polls);
 /* Last build's device time in milliseconds (CUDA events on the ctx stream). */
 int  ptgpu_last_build_ms(ptgpu_ctx *ctx, float *ms);
 
@@ -347,10 +374,11 @@ int  ptgpu_server_info_get(ptgpu_server *s, ptgpu_server_info *info);
  * a frame loop that must not stall on cudaMalloc/cudaFree, a plug-in host that
  * forbids it): intermediates live in a fixed array inside the library, so
  * n <= 262144 (PTGPU_E_RANGE beyond).  d_btn holds at least one node when
- * n == 1.  The first call on a device sets up that device's array; a caller
- * that captures streams makes it before any capture.  Calls that overlap on
- * the GPU share the array and race: serialise them.  Enqueued on `stream`
- * (cudaStream_t, NULL = legacy default); returns after the build finished.  */
+ * n == 1; nothing is written past btn[max(n-1,1)-1] or btl[n-1].  The first
+ * call on a device sets up that device's array: make it before any stream
+ * capture.  Calls that overlap on the GPU share the array and race: serialise
+ * them.  Enqueued on `stream` (cudaStream_t, NULL = legacy default); every
+ * call waits on the host for its build to finish before it returns.  */
 int  ptgpu_build_bvh_noalloc(const ptgpu_shape *d_shapes, uint32_t n,
                              ptgpu_bvh_node *d_btn, ptgpu_bvh_node *d_btl,
                              void *stream);
@@ -381,6 +409,8 @@ PTGPU_SA(sizeof(ptgpu_bvh_node) == 60, "BVHNodeGPU is 60 bytes");
 PTGPU_SA(offsetof(ptgpu_bvh_node, bound) == 28, "BVHNodeGPU.bound at 28");
 PTGPU_SA(sizeof(ptgpu_kd_node) == 36, "KDNodeGPU is 36 bytes");
 PTGPU_SA(offsetof(ptgpu_kd_node, min) == 32, "KDNodeGPU.min at 32");
+PTGPU_SA(sizeof(ptgpu_kd_node_wide) == 48, "wide KD node is 48 bytes");
+PTGPU_SA(offsetof(ptgpu_kd_node_wide, min) == 40, "wide KD node min at 40");
 /* the batch structs (no reference counterpart): fixed for foreign bindings */
 PTGPU_SA(sizeof(ptgpu_scene) == 120, "ptgpu_scene is 120 bytes");
 PTGPU_SA(offsetof(ptgpu_scene, camera) == 16, "ptgpu_scene.camera at 16");

@@ -179,6 +179,11 @@ float orc_triangle_intersect(const ptgpu_triangle *tr, const ptgpu_ray *r) {
 }
 
 int orc_bound_test(const ptgpu_ray *r, const ptgpu_bound *b) {
+    float tmin, tmax;
+    return orc_bound_test_t(r, b, &tmin, &tmax);
+}
+
+int orc_bound_test_t(const ptgpu_ray *r, const ptgpu_bound *b, float *tmin_out, float *tmax_out) {
     float xa = 1.f / r->d.x, ya = 1.f / r->d.y, za = 1.f / r->d.z;
     float xe = r->o.x, ye = r->o.y, ze = r->o.z;
     float txmin, txmax, tymin, tymax, tzmin, tzmax;
@@ -190,7 +195,18 @@ int orc_bound_test(const ptgpu_ray *r, const ptgpu_bound *b) {
     else         { tzmin = (b->max_z - ze) * za; tzmax = (b->min_z - ze) * za; }
     float tmin = fmaxf(txmin, fmaxf(tymin, tzmin));
     float tmax = fminf(txmax, fminf(tymax, tzmax));
+    *tmin_out = tmin;
+    *tmax_out = tmax;
     return tmin <= tmax;
+}
+
+/* cull_closest: a box the walk may skip (see orc_accel) */
+static inline int orc_box_enter(const orc_accel *acc, const ptgpu_ray *r, const ptgpu_bound *b,
+                                float tbest) {
+    float tmin, tmax;
+    if (!orc_bound_test_t(r, b, &tmin, &tmax)) return 0;
+    if (acc->cull_closest && (tmax < 0.f || tmin > tbest * 1.0001f)) return 0;
+    return 1;
 }
 
 static inline float shape_intersect(const ptgpu_shape *s, const ptgpu_ray *r) {
@@ -236,7 +252,7 @@ int orc_intersect(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
             }
             const ptgpu_bvh_node *nd = &btn[item];
             if (cnt) cnt->node_visits++;
-            if (!orc_bound_test(r, &nd->bound)) continue;
+            if (!orc_box_enter(acc, r, &nd->bound, *t)) continue;
             int lleaf, rleaf;
             if (acc->bvh_reference_leafness) {
                 lleaf = rleaf = (nd->leaf == 2);
@@ -256,7 +272,7 @@ int orc_intersect(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
     while (top > 0) {
         int32_t nidx = stack[--top];
         if (cnt) cnt->node_visits++;
-        if (!orc_bound_test(r, &acc->kd_box[nidx])) continue;
+        if (!orc_box_enter(acc, r, &acc->kd_box[nidx], *t)) continue;
         if (acc->kd_leaf[nidx] == 0) {
             if (acc->kd_left[nidx] < 0) continue; /* empty root (N == 0) */
             if (top + 2 > ORC_STACK_MAX) return 0;
@@ -283,6 +299,77 @@ int orc_intersect_p(const ptgpu_shape *shapes, uint32_t n, const ptgpu_ray *r, f
         if (d != 0.f && d < maxt) return 1;
     }
     return 0;
+}
+
+/* IntersectP's predicate answered through the tree: a depth-first walk with
+ * the reference's bound test (intersection_bound_test, no t culling, so it
+ * enters every box the brute-force loop could find a hit in) that stops at
+ * the first shape other than the last one with 0 < d < maxt.  An oracle-side
+ * speed-up only: the reference tests every shape (rendering_kernel.cl:375-395). */
+int orc_intersect_p_accel(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
+                          const ptgpu_ray *r, float maxt) {
+    if (!acc || !acc->shadow_accel || acc->accel == PTGPU_ACCEL_NONE ||
+        (acc->accel == PTGPU_ACCEL_BVH && n <= 1))
+        return orc_intersect_p(shapes, n, r, maxt);
+    if (n <= 1) return 0;
+    const uint32_t skip = n - 1;
+    int32_t stack[ORC_STACK_MAX];
+    int top = 0;
+    if (acc->accel == PTGPU_ACCEL_BVH) {
+        const ptgpu_bvh_node *btn = acc->btn, *btl = acc->btl;
+        stack[top++] = 0;
+        while (top > 0) {
+            int32_t item = stack[--top];
+            if (item < 0) {
+                uint32_t sid = (uint32_t)btl[-item - 1].nShape;
+                if (sid == skip) continue;
+                float d = shape_intersect(&shapes[sid], r);
+                if (d != 0.f && d < maxt) return 1;
+                continue;
+            }
+            const ptgpu_bvh_node *nd = &btn[item];
+            if (!orc_bound_test(r, &nd->bound)) continue;
+            int lleaf = (nd->nLeft == nd->min), rleaf = (nd->nRight == nd->max);
+            if (top + 2 > ORC_STACK_MAX) return orc_intersect_p(shapes, n, r, maxt);
+            stack[top++] = rleaf ? -(nd->nRight + 1) : nd->nRight;
+            stack[top++] = lleaf ? -(nd->nLeft + 1) : nd->nLeft;
+        }
+        return 0;
+    }
+    stack[top++] = acc->kd_root;
+    while (top > 0) {
+        int32_t nidx = stack[--top];
+        if (!orc_bound_test(r, &acc->kd_box[nidx])) continue;
+        if (acc->kd_leaf[nidx] == 0) {
+            if (acc->kd_left[nidx] < 0) continue;
+            if (top + 2 > ORC_STACK_MAX) return orc_intersect_p(shapes, n, r, maxt);
+            stack[top++] = acc->kd_right[nidx];
+            stack[top++] = acc->kd_left[nidx];
+        } else {
+            for (int32_t i = acc->kd_min[nidx]; i < acc->kd_max[nidx]; i++) {
+                uint32_t sid = (uint32_t)acc->kd_kn[i];
+                if (sid == skip) continue;
+                float d = shape_intersect(&shapes[sid], r);
+                if (d != 0.f && d < maxt) return 1;
+            }
+        }
+    }
+    return 0;
+}
+
+void orc_shadow_batch(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
+                      const ptgpu_ray *rays, const float *maxt, uint32_t nrays,
+                      int32_t *occluded, int threads) {
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+    #pragma omp parallel for schedule(dynamic, 256) num_threads(threads)
+#else
+    (void)threads;
+#endif
+    for (int64_t i = 0; i < (int64_t)nrays; ++i)
+        occluded[i] = (acc && acc->shadow_accel)
+                          ? orc_intersect_p_accel(shapes, n, acc, &rays[i], maxt[i])
+                          : orc_intersect_p(shapes, n, &rays[i], maxt[i]);
 }
 
 void orc_trace_closest(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
@@ -319,15 +406,27 @@ static void two_randoms(uint32_t *s0, uint32_t *s1, int rtl, float *u1, float *u
     else     { *u1 = orc_get_random(s0, s1); *u2 = orc_get_random(s0, s1); }
 }
 
-static void sample_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
+/* The emitters SampleLights visits: shapes with e != 0 in index order, until
+ * lightCnt of them (rendering_kernel.cl:403-407).  Collected once per pass
+ * instead of scanning the shape list at every diffuse hit; the order and the
+ * set are the scan's.  Returns the count written to lights[]. */
+static uint32_t collect_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
+                               uint32_t *lights) {
+    uint32_t i, visited;
+    for (i = 0, visited = 0; i < n && visited < light_cnt; i++) {
+        if (viszero(shapes[i].e)) continue;
+        lights[visited++] = i;
+    }
+    return visited;
+}
+
+static void sample_lights(const ptgpu_shape *shapes, uint32_t n, const uint32_t *lights,
+                          uint32_t n_lights, const orc_accel *acc,
                           int rtl, uint32_t *s0, uint32_t *s1, ptgpu_vec hit,
                           ptgpu_vec normal, ptgpu_vec *result) {
     *result = v3(0.f, 0.f, 0.f);
-    uint32_t i, visited;
-    for (i = 0, visited = 0; i < n && visited < light_cnt; i++) {
-        const ptgpu_shape *light = &shapes[i];
-        if (viszero(light->e)) continue;
-        visited++;
+    for (uint32_t li = 0; li < n_lights; li++) {
+        const ptgpu_shape *light = &shapes[lights[li]];
         ptgpu_ray shadow;
         shadow.o = hit;
         ptgpu_vec lp, ln;
@@ -362,7 +461,7 @@ static void sample_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_
         wo = -wo;
         wo = cl_clamp(wo, 0.f, 1.f);
         const float wi = vdot(shadow.d, normal);
-        if (wi > 0.f && !orc_intersect_p(shapes, n, &shadow, len - ORC_EPSILON)) {
+        if (wi > 0.f && !orc_intersect_p_accel(shapes, n, acc, &shadow, len - ORC_EPSILON)) {
             const float s = light->area * wi * wo / (len * len);
             *result = vadd(*result, vsmul(s, light->e));
         }
@@ -370,10 +469,24 @@ static void sample_lights(const ptgpu_shape *shapes, uint32_t n, uint32_t light_
 }
 
 /* RadianceOnePathTracing + RadiancePathTracing (rendering_kernel.cl:495-820) */
+static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *lights,
+                     uint32_t n_lights, const orc_accel *acc, int max_depth, int rtl,
+                     const ptgpu_ray *start, uint32_t *s0, uint32_t *s1, ptgpu_vec *result);
+
 void orc_radiance(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
                   const orc_accel *acc, int max_depth, int rtl,
                   const ptgpu_ray *start, uint32_t *s0, uint32_t *s1,
                   ptgpu_vec *result) {
+    uint32_t cap = light_cnt < n ? light_cnt : n;
+    uint32_t *lights = (uint32_t *)malloc(sizeof(uint32_t) * (cap ? cap : 1));
+    uint32_t nl = collect_lights(shapes, n, light_cnt, lights);
+    radiance(shapes, n, lights, nl, acc, max_depth, rtl, start, s0, s1, result);
+    free(lights);
+}
+
+static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *lights,
+                     uint32_t n_lights, const orc_accel *acc, int max_depth, int rtl,
+                     const ptgpu_ray *start, uint32_t *s0, uint32_t *s1, ptgpu_vec *result) {
     ptgpu_ray ray = *start;
     ptgpu_vec rad = v3(0.f, 0.f, 0.f);
     ptgpu_vec tp = v3(1.f, 1.f, 1.f);
@@ -406,7 +519,7 @@ void orc_radiance(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
             specular = 0;
             tp = vmul(tp, col);
             ptgpu_vec ld;
-            sample_lights(shapes, n, light_cnt, rtl, s0, s1, hp, nl, &ld);
+            sample_lights(shapes, n, lights, n_lights, acc, rtl, s0, s1, hp, nl, &ld);
             ld = vmul(ld, tp);
             rad = vadd(rad, ld);
             float r1 = 2.f * ORC_PI * orc_get_random(s0, s1);
@@ -481,9 +594,14 @@ void orc_render_pass(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
     if (row_end > h) row_end = h;
     if (col_end > w || col_end <= 0) col_end = w;
     if (col_begin < 0) col_begin = 0;
+    uint32_t cap = light_cnt < n ? light_cnt : n;
+    uint32_t *lights = (uint32_t *)malloc(sizeof(uint32_t) * (cap ? cap : 1));
+    const uint32_t n_lights = collect_lights(shapes, n, light_cnt, lights);
 #ifdef _OPENMP
     if (threads <= 0) threads = omp_get_max_threads();
-    #pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+    /* pixels are independent (each has its own seed stream): rows and
+     * columns are shared out together, so one row also uses every thread */
+    #pragma omp parallel for collapse(2) schedule(dynamic, 8) num_threads(threads)
 #else
     (void)threads;
 #endif
@@ -494,7 +612,7 @@ void orc_render_pass(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
             ptgpu_ray ray;
             orc_generate_camera_ray(cam, &s0, &s1, w, h, x, y, &ray);
             ptgpu_vec r;
-            orc_radiance(shapes, n, light_cnt, acc, max_depth, rtl, &ray, &s0, &s1, &r);
+            radiance(shapes, n, lights, n_lights, acc, max_depth, rtl, &ray, &s0, &s1, &r);
             const int i = (h - y - 1) * w + x;
             if (current_sample == 0) {
                 colors[i] = r;
@@ -512,6 +630,7 @@ void orc_render_pass(const ptgpu_shape *shapes, uint32_t n, uint32_t light_cnt,
             seeds[2 * gid + 1] = s1;
         }
     }
+    free(lights);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -32,6 +32,18 @@ typedef struct {
     const int32_t *kd_min, *kd_max;  /* leaf ranges into kd_kn              */
     const int32_t *kd_kn;
     int32_t kd_root;
+    /* 0: shadow rays by the reference's brute-force IntersectP; 1: the same
+     * predicate (any shape but the last with 0 < d < maxt) answered through
+     * the BVH or KD tree above, for scenes where brute force is too slow on
+     * the CPU.  The two are compared on the CPU by the test suite. */
+    int32_t shadow_accel;
+    /* 1: the closest-hit walk (BVH/KD) skips a box whose entry distance is
+     * beyond the best hit so far by more than rounding (1e-4 relative) or whose
+     * exit lies behind the origin.  No box it skips can hold a hit the walk
+     * would keep, and the visit order is unchanged, so results are the
+     * reference walk's; another oracle-side speed-up, compared on the CPU by
+     * the test suite. */
+    int32_t cull_closest;
 } orc_accel;
 
 /* RNG and camera */
@@ -46,10 +58,20 @@ void  orc_make_seeds(uint64_t master, uint32_t *seeds, uint32_t count);
 float orc_sphere_intersect(const ptgpu_sphere *s, const ptgpu_ray *r);
 float orc_triangle_intersect(const ptgpu_triangle *tr, const ptgpu_ray *r);
 int   orc_bound_test(const ptgpu_ray *r, const ptgpu_bound *b);
+/* the same test, also returning the entry and exit distances */
+int   orc_bound_test_t(const ptgpu_ray *r, const ptgpu_bound *b, float *tmin, float *tmax);
 int   orc_intersect(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
                     const ptgpu_ray *r, float *t, uint32_t *id, orc_counters *cnt);
 int   orc_intersect_p(const ptgpu_shape *shapes, uint32_t n, const ptgpu_ray *r,
                       float maxt);
+int   orc_intersect_p_accel(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
+                            const ptgpu_ray *r, float maxt);
+/* one shadow query per ray (maxt[i]); occluded[i] = 1 when any shape but the
+ * last is hit at 0 < d < maxt[i]; accel == NULL or shadow_accel == 0: brute
+ * force */
+void  orc_shadow_batch(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
+                       const ptgpu_ray *rays, const float *maxt, uint32_t nrays,
+                       int32_t *occluded, int threads);
 void  orc_trace_closest(const ptgpu_shape *shapes, uint32_t n, const orc_accel *acc,
                         const ptgpu_ray *rays, uint32_t nrays, float *t,
                         uint32_t *id, int32_t *hit, orc_counters *cnt, int threads);

@@ -7,7 +7,9 @@
 # never reaches t = 0 and ends in an integer division by zero on the CPU).
 # Everything written goes under oracle/_ref/, which git ignores.
 set -euo pipefail
-REF=${PTGPU_REFERENCE_DIR:-/root/reference}
+# the reference tree is named only by PTGPU_REFERENCE_DIR
+REF=${PTGPU_REFERENCE_DIR:-}
+if [ -z "$REF" ]; then echo "PTGPU_REFERENCE_DIR is not set: the reference build is skipped" >&2; exit 3; fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$(cd "$HERE/.." && pwd)/_ref
 if [ ! -f "$REF/include/BVH.cl" ]; then echo "reference tree not found at $REF" >&2; exit 3; fi

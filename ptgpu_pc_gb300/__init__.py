@@ -20,7 +20,7 @@ EXPORTS = [
     "ptgpu_create", "ptgpu_destroy", "ptgpu_status_string", "ptgpu_last_error",
     "ptgpu_abi_version", "ptgpu_read_scene", "ptgpu_stream_scene", "ptgpu_set_shapes", "ptgpu_get_shape_count",
     "ptgpu_get_shapes", "ptgpu_update_camera", "ptgpu_set_camera", "ptgpu_get_camera",
-    "ptgpu_build", "ptgpu_get_bvh", "ptgpu_get_kdtree", "ptgpu_set_bvh", "ptgpu_last_build_ms",
+    "ptgpu_build", "ptgpu_get_bvh", "ptgpu_get_kdtree", "ptgpu_get_kdtree_wide", "ptgpu_set_bvh", "ptgpu_last_build_ms", "ptgpu_set_wait_limit",
     "ptgpu_make_seeds", "ptgpu_set_seeds", "ptgpu_get_seeds", "ptgpu_reset_accumulation",
     "ptgpu_draw_frame", "ptgpu_render_async", "ptgpu_synchronize", "ptgpu_get_colors",
     "ptgpu_get_pixels", "ptgpu_get_current_sample", "ptgpu_trace_closest",
@@ -93,7 +93,9 @@ def lib():
         L.ptgpu_get_bvh.argtypes = [vp, vp, vp]
         L.ptgpu_set_bvh.argtypes = [vp, vp, vp, u32]
         L.ptgpu_get_kdtree.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]
+        L.ptgpu_get_kdtree_wide.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]
         L.ptgpu_last_build_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+        L.ptgpu_set_wait_limit.argtypes = [vp, u32]
         L.ptgpu_make_seeds.argtypes = [ctypes.c_uint64, vp, u32]
         L.ptgpu_set_seeds.argtypes = [vp, vp]
         L.ptgpu_get_seeds.argtypes = [vp, vp]
@@ -215,6 +217,11 @@ class Context:
     def build(self, accel=abi.ACCEL_BVH, flags=0):
         _check(lib().ptgpu_build(self._h, accel, flags))
 
+    def set_wait_limit(self, polls):
+        """Look-back polls before a build gives up with E_TIMEOUT (0: at the
+        first wait; abi.WAIT_LIMIT_DEFAULT restores the default)."""
+        _check(lib().ptgpu_set_wait_limit(self._h, int(polls)))
+
     def last_build_ms(self):
         ms = ctypes.c_float()
         _check(lib().ptgpu_last_build_ms(self._h, ctypes.byref(ms)))
@@ -239,6 +246,15 @@ class Context:
         kn = np.zeros(max(nc.value, 1), np.int32)
         _check(lib().ptgpu_get_kdtree(self._h, _p(kng), ctypes.byref(kc), _p(kn), ctypes.byref(nc)))
         return kng, kn[: nc.value]
+
+    def get_kdtree_wide(self):
+        """Returns (nodes, kn): the KD tree breadth-first with 32-bit fields."""
+        kc, nc = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().ptgpu_get_kdtree_wide(self._h, None, ctypes.byref(kc), None, ctypes.byref(nc)))
+        nodes = np.zeros(max(kc.value, 1), abi.KD_NODE_WIDE)
+        kn = np.zeros(max(nc.value, 1), np.int32)
+        _check(lib().ptgpu_get_kdtree_wide(self._h, _p(nodes), ctypes.byref(kc), _p(kn), ctypes.byref(nc)))
+        return nodes[: kc.value], kn[: nc.value]
 
     def set_seeds(self, seeds):
         seeds = np.ascontiguousarray(seeds, np.uint32)

@@ -10,6 +10,7 @@ import numpy as np
 SPHERE, TRIANGLE = 0, 1
 DIFF, SPEC, REFR = 0, 1, 2
 ACCEL_NONE, ACCEL_BVH, ACCEL_KDTREE = 0, 1, 2
+WAIT_LIMIT_DEFAULT = 4194304      # PTGPU_WAIT_LIMIT_DEFAULT
 
 VEC = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4")])
 RAY = np.dtype({"names": ["o", "d"], "formats": [("<f4", 3), ("<f4", 3)],
@@ -46,6 +47,13 @@ KD_NODE = np.dtype({
     "formats": ["<i2"] * 4 + [("<f4", 6), "<i2", "<i2"],
     "offsets": [0, 2, 4, 6, 8, 32, 34],
     "itemsize": 36,
+})
+
+KD_NODE_WIDE = np.dtype({
+    "names": ["leaf", "nLeft", "nRight", "nParent", "bound", "min", "max"],
+    "formats": ["<i4"] * 4 + [("<f4", 6), "<i4", "<i4"],
+    "offsets": [0, 4, 8, 12, 16, 40, 44],
+    "itemsize": 48,
 })
 
 CONFIG = np.dtype({

@@ -85,6 +85,7 @@ struct ptgpu_ctx {
     int accel_cfg = PTGPU_ACCEL_BVH;
     int block = 128;
     int flags = 0;
+    uint32_t wait_limit = kDefaultWaitLimit;   // look-back polls before E_TIMEOUT
     // scene
     // the scene's shape records: d_shapes holds them as set (never modified);
     // the host copy is made from it only when a call needs one
@@ -496,6 +497,7 @@ static int ptgpu_build_body(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
         b.arrivals = c->d_arrivals.as<uint32_t>();
         b.btn = c->d_btn.as<ptgpu_bvh_node>();
         b.btl = c->d_btl.as<ptgpu_bvh_node>();
+        b.wait_limit = c->wait_limit;
         CK(cudaEventRecord(c->ev0, c->stream));
         CK(launch_lbvh_build(b, (int)c->n, c->all_tri ? 1 : 0, c->sm_count, c->stream));
         if (flags & PTGPU_FLAG_TREELET) {
@@ -561,6 +563,14 @@ static int ptgpu_build_body(ptgpu_ctx *c, int32_t accel, uint32_t flags) {
     return PTGPU_OK;
 }
 
+static_assert(PTGPU_WAIT_LIMIT_DEFAULT == kDefaultWaitLimit, "header and build agree on the default");
+
+int ptgpu_set_wait_limit(ptgpu_ctx *c, uint32_t polls) {
+    if (!c) return fail(PTGPU_E_INVAL, "null context");
+    c->wait_limit = polls;
+    return PTGPU_OK;
+}
+
 int ptgpu_last_build_ms(ptgpu_ctx *c, float *ms) {
     if (!c || !ms) return fail(PTGPU_E_INVAL, "null argument");
     *ms = c->last_build_ms;
@@ -620,6 +630,25 @@ int ptgpu_get_kdtree(ptgpu_ctx *c, ptgpu_kd_node *kng, int32_t *kng_cnt, int32_t
     *kng_cnt = (int32_t)size;
     st = kd_export_heap(c->kd, kng, size, kn);
     if (st) return fail(st, "KD tree does not fit the int16 layout");
+    return PTGPU_OK;
+}
+
+int ptgpu_get_kdtree_wide(ptgpu_ctx *c, ptgpu_kd_node_wide *nodes, int32_t *node_cnt, int32_t *kn,
+                          int32_t *kn_cnt) {
+    if (!c || !node_cnt || !kn_cnt) return fail(PTGPU_E_INVAL, "null argument");
+    if (!c->kd_valid) return fail(PTGPU_E_STATE, "no KD tree has been built");
+    const int32_t cnt = c->kd.node_count();
+    const int32_t kcnt = (int32_t)c->kd.kn.size();
+    if (!nodes || !kn) {          // size query
+        *node_cnt = cnt;
+        *kn_cnt = kcnt;
+        return PTGPU_OK;
+    }
+    if (*node_cnt < cnt || *kn_cnt < kcnt) return fail(PTGPU_E_INVAL, "node or kn buffer too small");
+    kd_export_wide(c->kd, nodes);
+    if (kcnt) std::memcpy(kn, c->kd.kn.data(), sizeof(int32_t) * (size_t)kcnt);
+    *node_cnt = cnt;
+    *kn_cnt = kcnt;
     return PTGPU_OK;
 }
 

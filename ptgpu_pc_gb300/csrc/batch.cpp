@@ -312,6 +312,7 @@ static int ptgpu_batch_build_body(ptgpu_batch *b, uint32_t flags) {
     // the build: every tree in one pass of the LBVH kernels
     LbvhBuffers lb;
     std::memset(&lb, 0, sizeof(lb));
+    lb.wait_limit = kDefaultWaitLimit;
     lb.verts = b->d_verts.as<float>();
     lb.type = b->d_type.as<uint8_t>();
     lb.aabbs = b->d_aabbs.as<float4>();

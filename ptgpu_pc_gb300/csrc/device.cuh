@@ -263,7 +263,10 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
                     if (dd < q.tb) { q.hit = 1; return true; }
                 } else {
                     q.hit = 1;
-                    if (dd < q.tb) { q.tb = dd; q.prim = k; }
+                    // equal t: the lower traversal-order index wins, which in
+                    // the BVH is the leaf the reference's left-first walk
+                    // meets first (its `d < t` keeps the first one found)
+                    if (dd < q.tb || (dd == q.tb && k < q.prim)) { q.tb = dd; q.prim = k; }
                 }
             }
         }

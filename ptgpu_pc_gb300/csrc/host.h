@@ -27,6 +27,8 @@ int kd_build(const ptgpu_shape *shapes, uint32_t n, KdTree &out);
 // the int16 fields (the arrays are still filled, truncated like the reference).
 int kd_heap_size(const KdTree &kd, int64_t *kng_cnt);
 int kd_export_heap(const KdTree &kd, ptgpu_kd_node *kng, int64_t kng_cnt, int32_t *kn);
+// The tree breadth-first with 32-bit fields (nodes must hold node_count()).
+void kd_export_wide(const KdTree &kd, ptgpu_kd_node_wide *nodes);
 // Traversal layout: 16 floats per internal node (see device.cuh), internal
 // nodes numbered breadth-first; a root leaf is returned through root_first /
 // root_count with no internal nodes.

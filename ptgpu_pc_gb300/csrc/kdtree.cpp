@@ -195,6 +195,38 @@ int kd_export_heap(const KdTree &kd, ptgpu_kd_node *kng, int64_t kng_cnt, int32_
     return st;
 }
 
+void kd_export_wide(const KdTree &kd, ptgpu_kd_node_wide *nodes) {
+    // breadth-first numbering: the heap export's order with its empty slots
+    // left out
+    const int32_t cnt = kd.node_count();
+    if (cnt == 0) return;
+    std::vector<int32_t> order;
+    std::vector<int32_t> bfs(cnt, -1);
+    order.reserve(cnt);
+    order.push_back(0);
+    bfs[0] = 0;
+    for (size_t h = 0; h < order.size(); ++h) {
+        const int32_t nd = order[h];
+        for (int32_t c : {kd.left[nd], kd.right[nd]})
+            if (c >= 0) { bfs[c] = (int32_t)order.size(); order.push_back(c); }
+    }
+    for (int32_t i = 0; i < (int32_t)order.size(); ++i) {
+        const int32_t nd = order[i];
+        ptgpu_kd_node_wide &k = nodes[i];
+        k.leaf = kd.leaf[nd];
+        k.nLeft = kd.left[nd] >= 0 ? bfs[kd.left[nd]] : -1;
+        k.nRight = kd.right[nd] >= 0 ? bfs[kd.right[nd]] : -1;
+        k.nParent = -1;
+        k.bound = kd.box[nd];
+        k.min = kd.leaf[nd] ? kd.kmin[nd] : 0;
+        k.max = kd.leaf[nd] ? kd.kmax[nd] : 0;
+    }
+    for (int32_t i = 0; i < (int32_t)order.size(); ++i) {
+        if (nodes[i].nLeft >= 0) nodes[nodes[i].nLeft].nParent = i;
+        if (nodes[i].nRight >= 0) nodes[nodes[i].nRight].nParent = i;
+    }
+}
+
 void kd_trace_nodes(const KdTree &kd, std::vector<float> &nodes, int32_t *root_first,
                     int32_t *root_count, float root_box[6]) {
     nodes.clear();

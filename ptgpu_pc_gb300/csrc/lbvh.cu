@@ -23,6 +23,7 @@
 #include <cfloat>
 #include <cstring>
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -130,13 +131,14 @@ __device__ __forceinline__ void pdl_begin() {
 #endif
 }
 
-__global__ void k_init_state(BuildState *st) {
+__global__ void k_init_state(BuildState *st, uint32_t wait_limit) {
     int t = threadIdx.x;
     for (int i = t; i < 5 * 256; i += blockDim.x) (&st->hist[0][0])[i] = 0u;
     if (t < 5) st->tile_counter[t] = 0u;
     if (t == 0) {
         st->error = 0u;
         st->top_ticket = 0u;
+        st->wait_limit = wait_limit;
         // the reference's initial values: FLT_MAX for minima, FLT_MIN for maxima
         for (int a = 0; a < 3; ++a) {
             st->cmin[a] = f2ord(FLT_MAX);
@@ -149,7 +151,7 @@ __global__ void k_init_state(BuildState *st) {
 // arrival counters of a single-tree build, cleared in one launch (block 0
 // also writes the state's initial values).
 __global__ void k_init_build(BuildState *st, uint4 *__restrict__ status, size_t status_quads,
-                             uint32_t *__restrict__ arrivals, size_t arrival_words) {
+                             uint32_t *__restrict__ arrivals, size_t arrival_words, uint32_t wait_limit) {
     if (blockIdx.x == 0) {
         const int t = threadIdx.x;
         for (int i = t; i < 5 * 256; i += blockDim.x) (&st->hist[0][0])[i] = 0u;
@@ -157,6 +159,7 @@ __global__ void k_init_build(BuildState *st, uint4 *__restrict__ status, size_t 
         if (t == 0) {
             st->error = 0u;
             st->top_ticket = 0u;
+            st->wait_limit = wait_limit;
             for (int a = 0; a < 3; ++a) {   // the reference's FLT_MAX / FLT_MIN initial values
                 st->cmin[a] = f2ord(FLT_MAX);
                 st->cmax[a] = f2ord(FLT_MIN);
@@ -576,7 +579,6 @@ constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = PTGPU_SORT_ITEMS;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1u;
-constexpr int kSpinLimit = 1 << 22;
 #ifndef PTGPU_LOOKBACK
 #define PTGPU_LOOKBACK 8
 #endif
@@ -629,8 +631,11 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_t
 // Decoupled look-back of one digit (one thread per digit): publishes the
 // tile's count as an aggregate (tile 0: as inclusive), sums predecessors back
 // to the first inclusive word and publishes the inclusive count.  Returns the
-// count of this digit in all earlier tiles; a wait past kSpinLimit sets the
-// build's error bit and the tile's abort flag.
+// count of this digit in all earlier tiles.  A tile that has waited
+// st->wait_limit times (kDefaultWaitLimit unless the caller lowered it; 0
+// gives up before the first read) sets the build's error bit and its abort
+// flag: it then scatters nothing, and every later kernel stays in bounds
+// (destinations are checked against n, gathered indices clamped to [0, n)).
 __device__ __forceinline__ uint32_t lookback_digit(uint32_t *status, int tile, int tid, uint32_t count,
                                                    BuildState *st, int &abort_flag) {
     uint32_t *my = status + (size_t)tile * 256 + tid;
@@ -645,8 +650,10 @@ __device__ __forceinline__ uint32_t lookback_digit(uint32_t *status, int tile, i
     // ends the window and is read again
     int p = tile - 1;
     bool timed_out = false;
-    int spins = 0;
+    const uint32_t limit = st->wait_limit;
+    uint32_t spins = 0;
     while (p >= 0) {
+        if (spins >= limit) { timed_out = true; break; }
         uint32_t v[kLookback];
 #pragma unroll
         for (int q = 0; q < kLookback; ++q)
@@ -663,7 +670,7 @@ __device__ __forceinline__ uint32_t lookback_digit(uint32_t *status, int tile, i
         if (done) break;
         p -= q;
         if (q < kLookback) {
-            if (++spins > kSpinLimit) { timed_out = true; break; }
+            ++spins;
             __nanosleep(32);
         }
     }
@@ -1939,12 +1946,16 @@ static cudaError_t launch_chained(void (*k)(P...), int grid, int block, size_t s
     return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
-// shared-memory opt-ins of the build kernels, once per device
+// shared-memory opt-ins of the build kernels, once per device; contexts,
+// batches, the server's worker and the no-allocation entry point may build
+// from different host threads at once, so the per-device flags are guarded
 static cudaError_t launch_lbvh_prepare_attrs() {
+    static std::mutex attr_mutex;
     static bool attr_set[64] = {false};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(attr_mutex);
     if (dev >= 0 && dev < 64 && attr_set[dev]) return cudaSuccess;
     const size_t smem = sizeof(SortSmem);
     sort_attrs(k_onesweep<true, false>, smem);
@@ -1953,8 +1964,9 @@ static cudaError_t launch_lbvh_prepare_attrs() {
     sort_attrs(k_onesweep<false, true, true>, smem);
     cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
     cudaFuncSetAttribute(k_tiles_seg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
-    if (dev >= 0 && dev < 64) attr_set[dev] = true;
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e == cudaSuccess && dev >= 0 && dev < 64) attr_set[dev] = true;
+    return e;
 }
 
 cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_count,
@@ -1968,7 +1980,8 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
     // status words: a multiple of 4 (tiles * 256 * 5), cleared as 16-byte words
     if (reinterpret_cast<uintptr_t>(b.status) & 15) return cudaErrorInvalidValue;
     k_init_build<<<sm_count * 2, 256, 0, s>>>(b.state, reinterpret_cast<uint4 *>(b.status),
-                                              sort_status_words(n) / 4, b.arrivals, block_bound_count(n));
+                                              sort_status_words(n) / 4, b.arrivals, block_bound_count(n),
+                                              b.wait_limit);
     const int red_grid = grid_for(n, 256, sm_count * 8);
     e = launch_chained(k_centroid_bounds, red_grid, 256, 0, s, (const float *)b.verts, (const uint8_t *)b.type,
                        all_tri, n, b.state, b.aabbs);
@@ -2033,7 +2046,7 @@ cudaError_t launch_lbvh_build_seg(const LbvhBuffers &b, int n, const SegBuild &s
     if (e != cudaSuccess) return e;
     const int ntiles_sort = (n + kSortTile - 1) / kSortTile;
     const size_t smem = sizeof(SortSmem);
-    k_init_state<<<1, 256, 0, s>>>(b.state);
+    k_init_state<<<1, 256, 0, s>>>(b.state, b.wait_limit);
     k_seg_init<<<(sb.n_segs + 127) / 128, 128, 0, s>>>(sb.seg_state, sb.n_segs, b.state, sb.seg_off);
     e = cudaMemsetAsync(b.status, 0, sort_status_words(n) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;

@@ -20,7 +20,12 @@ struct BuildState {
     uint32_t cmin[3], cmax[3];  // centroid bounds as order-preserving uints
     uint32_t error;             // bit 0: a look-back wait gave up
     uint32_t top_ticket;
+    uint32_t wait_limit;        // polls a look-back may wait before it gives up
 };
+
+// Polls (about 32 ns apart) a radix-sort look-back waits for a predecessor
+// tile before the build gives up with PTGPU_E_TIMEOUT.
+constexpr uint32_t kDefaultWaitLimit = 1u << 22;
 
 struct LbvhBuffers {
     const float *verts;         // 9 floats per shape (p1,p2,p3 or centre,rad)
@@ -36,6 +41,7 @@ struct LbvhBuffers {
     float *block_bounds;        // 6 floats per block at the tile level and above
     uint32_t *arrivals;         // arrival counters of the blocks above the tiles
     ptgpu_bvh_node *btn, *btl;  // the reference's output arrays
+    uint32_t wait_limit = kDefaultWaitLimit;   // BuildState::wait_limit of the build
 };
 
 size_t sort_status_words(int n);   // look-back words of all (five) passes

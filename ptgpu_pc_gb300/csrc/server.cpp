@@ -196,7 +196,10 @@ int grow_pixels(ptgpu_server *s, int64_t need) {
 
 int grow_lights(ptgpu_server *s, int64_t need) {
     const int64_t cap = s->light_slots.capacity;
-    const int64_t want = std::max<int64_t>(std::max<int64_t>(cap * 2, cap + need), 256);
+    int64_t want = std::max<int64_t>(std::max<int64_t>(cap * 2, cap + need), 256);
+    const int64_t room = (s->budget - s->bytes_in_use()) / (int64_t)sizeof(LightRec) + cap;
+    if (want > room) want = room;
+    if (want < cap + need) return PTGPU_E_OOM;
     cudaError_t e = s->lights.grow(cap, want, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "light arena");
     s->light_slots.grow(want);
@@ -248,12 +251,27 @@ int build_scene(ptgpu_server *s, int id) {
     int64_t base = 0;
     if (!alloc_shapes(s, n, &base)) return record_error(PTGPU_E_OOM, "scene does not fit the budget");
     int64_t lbase = 0;
+    // The slots go back to their arenas on every failure below (a device
+    // error, a scene file that changed or vanished, a look-back timeout); only
+    // a scene that became resident keeps them, until it is evicted.
+    struct SlotGuard {
+        ptgpu_server *s;
+        int64_t base, n, lbase = 0, nl = 0;
+        bool keep = false;
+        ~SlotGuard() {
+            if (keep) return;
+            s->shape_slots.release(base, n);
+            if (nl > 0) s->light_slots.release(lbase, nl);
+        }
+    } guard{s, base, (int64_t)n};
     if (sc.n_lights > 0) {
         if (!s->light_slots.alloc((int64_t)sc.n_lights, &lbase)) {
-            int st = grow_lights(s, (int64_t)sc.n_lights);
-            if (st) return st;
-            s->light_slots.alloc((int64_t)sc.n_lights, &lbase);
+            if (grow_lights(s, (int64_t)sc.n_lights) != PTGPU_OK ||
+                !s->light_slots.alloc((int64_t)sc.n_lights, &lbase))
+                return record_error(PTGPU_E_OOM, "the scene's lights do not fit the budget");
         }
+        guard.lbase = lbase;
+        guard.nl = (int64_t)sc.n_lights;
         if (!sc.lights.empty())
             SK(cudaMemcpyAsync(s->lights.buf.as<LightRec>() + lbase, sc.lights.data(),
                                sc.lights.size() * sizeof(LightRec), cudaMemcpyHostToDevice, s->stream));
@@ -294,6 +312,7 @@ int build_scene(ptgpu_server *s, int id) {
                             prims0, s->mats.buf.as<Material>() + base, s->stream));
     LbvhBuffers b;
     std::memset(&b, 0, sizeof(b));
+    b.wait_limit = kDefaultWaitLimit;
     b.verts = s->s_verts.as<float>();
     b.type = s->s_type.as<uint8_t>();
     b.aabbs = s->s_aabbs.as<float4>();
@@ -338,6 +357,7 @@ int build_scene(ptgpu_server *s, int id) {
     sc.light_base = lbase;
     sc.depth = depth;
     sc.resident = true;
+    guard.keep = true;
     s->lru.push_back(id);
     sc.lru = std::prev(s->lru.end());
     std::lock_guard<std::mutex> lk(s->mu);

@@ -1,3 +1,4 @@
+import json
 import os
 import sys
 
@@ -29,3 +30,20 @@ def orc():
     import oracle
     oracle.build()
     return oracle
+
+
+@pytest.fixture(scope="session")
+def parity_report():
+    """Returns record(name, **numbers): appends one JSON line per call to the
+    file PTGPU_PARITY_REPORT names (nothing when it is unset), so a GPU run
+    can keep the measured parity figures (RMSE, identical fractions)."""
+    path = os.environ.get("PTGPU_PARITY_REPORT")
+
+    def record(name, **numbers):
+        line = dict(test=name, **{k: (float(v) if hasattr(v, "__float__") else v)
+                                  for k, v in numbers.items()})
+        print(json.dumps(line))
+        if path:
+            with open(path, "a") as f:
+                f.write(json.dumps(line) + "\n")
+    return record

@@ -65,6 +65,13 @@ int shim_kd_export(ptgpu_kd_node *kng, int64_t cnt, int32_t *kn) {
     return ptgpu::kd_export_heap(g_kd, kng, cnt, kn);
 }
 
+int shim_kd_node_count() { return g_kd.node_count(); }
+
+void shim_kd_export_wide(ptgpu_kd_node_wide *nodes, int32_t *kn) {
+    ptgpu::kd_export_wide(g_kd, nodes);
+    for (size_t i = 0; i < g_kd.kn.size(); ++i) kn[i] = g_kd.kn[i];
+}
+
 static ptgpu::LoadedScene g_scene;
 
 int shim_read_scene(const char *path, int w, int h, int *n, int *light_cnt, int *walllight,

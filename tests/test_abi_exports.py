@@ -42,7 +42,8 @@ def test_abi_version_without_a_device(built_lib):
 
 
 @pytest.mark.parametrize("name,size", [("SHAPE", 104), ("CAMERA", 76), ("BVH_NODE", 60),
-                                       ("KD_NODE", 36), ("CONFIG", 40), ("SCENE", 120),
+                                       ("KD_NODE", 36), ("KD_NODE_WIDE", 48), ("CONFIG", 40),
+                                       ("SCENE", 120),
                                        ("BATCH_INFO", 40), ("REQUEST", 112), ("REQUEST_STATS", 24),
                                        ("SERVER_INFO", 72)])
 def test_binding_struct_sizes(name, size):
@@ -50,7 +51,7 @@ def test_binding_struct_sizes(name, size):
     assert getattr(abi, name).itemsize == size
     text = open(HEADER).read()
     c = {"SHAPE": "ptgpu_shape", "CAMERA": "ptgpu_camera", "BVH_NODE": "ptgpu_bvh_node",
-         "KD_NODE": "ptgpu_kd_node", "SCENE": "ptgpu_scene", "BATCH_INFO": "ptgpu_batch_info",
+         "KD_NODE": "ptgpu_kd_node", "KD_NODE_WIDE": "ptgpu_kd_node_wide", "SCENE": "ptgpu_scene", "BATCH_INFO": "ptgpu_batch_info",
          "REQUEST": "ptgpu_request", "REQUEST_STATS": "ptgpu_request_stats",
          "SERVER_INFO": "ptgpu_server_info"}.get(name)
     if c:

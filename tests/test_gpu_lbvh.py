@@ -75,8 +75,10 @@ def test_lbvh_mixed_spheres_triangles(built_lib, orc):
     _compare(s[rng.permutation(len(s))], orc)
 
 
-@pytest.mark.parametrize("n", [1 << 20, (1 << 20) + 7])
+@pytest.mark.parametrize("n", [1 << 20, (1 << 20) + 7, 1 << 22])
 def test_lbvh_1m(n, built_lib, orc):
+    """Config 3's soups (1M and 4M triangles) and an odd size: Morton keys,
+    sorted order and both node arrays byte for byte."""
     _compare(scenes.triangle_soup(n, seed=5), orc)
 
 

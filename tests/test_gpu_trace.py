@@ -31,22 +31,54 @@ def _barycentric_margin(shapes, ids, rays, t):
     return m
 
 
-def _check(shapes, rays, g, o):
+def _check(shapes, rays, g, o, report=None, name=None):
+    """The closest-hit rule: every ray whose hit lies at least 1e-6
+    (barycentric) from the hit triangle's edges gets the same answer as the
+    oracle: the same hit flag, the same shape id, t within 1e-5 relative.
+    A ray is exempt only when the oracle's hit, or the GPU's where the two
+    disagree, lies within 1e-6 of an edge (shared-edge rays)."""
     gt, gid, ghit = g
     ot, oid, ohit = o
-    both = (ghit == 1) & (ohit == 1) & (gt < 1e20) & (ot < 1e20)
-    only = (ghit != ohit)
-    # disagreement on hit/miss only for grazing cases
-    assert only.mean() < 1e-4, "hit/miss disagree on %d rays" % only.sum()
-    rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
-    assert (rel <= T_RTOL).mean() > 0.9999, "t differs: max rel %g" % rel.max()
-    diff = both & (gid != oid)
-    if diff.any():
-        m_o = _barycentric_margin(shapes, oid[diff], rays[diff], ot[diff])
-        m_g = _barycentric_margin(shapes, gid[diff], rays[diff], gt[diff])
-        assert ((m_o < EDGE) | (m_g < EDGE) | (np.abs(gt[diff] - ot[diff]) == 0)).all(), \
-            "%d id mismatches away from edges" % diff.sum()
-    return both.sum(), diff.sum()
+    gh = (ghit == 1) & (gt < 1e20)
+    oh = (ohit == 1) & (ot < 1e20)
+    m_o = np.ones(len(rays))
+    m_g = np.ones(len(rays))
+    m_o[oh] = _barycentric_margin(shapes, oid[oh], rays[oh], ot[oh])
+    m_g[gh] = _barycentric_margin(shapes, gid[gh], rays[gh], gt[gh])
+    exempt = (oh & (m_o < EDGE)) | (gh & (m_g < EDGE))
+    flag_bad = (gh != oh) & ~exempt
+    both = gh & oh
+    id_bad = both & (gid != oid) & ~exempt
+    rel = np.zeros(len(rays))
+    rel[both] = np.abs(gt[both].astype(np.float64) - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
+    t_bad = both & (gid == oid) & (rel > T_RTOL) & ~exempt
+    if report is not None:
+        report(name, rays=len(rays), hits=int(oh.sum()), exempt=int(exempt.sum()),
+               id_equal_frac=float((gid[both] == oid[both]).mean()) if both.any() else 1.0,
+               max_rel_t=float(rel[both & ~exempt].max()) if (both & ~exempt).any() else 0.0,
+               flag_bad=int(flag_bad.sum()), id_bad=int(id_bad.sum()), t_bad=int(t_bad.sum()))
+    assert not flag_bad.any(), "hit/miss differ on %d rays away from edges" % flag_bad.sum()
+    assert not id_bad.any(), "%d id mismatches away from edges" % id_bad.sum()
+    assert not t_bad.any(), "t differs beyond 1e-5 on %d rays (max %g)" % (t_bad.sum(), rel[t_bad].max())
+    return int(both.sum()), int(((gid != oid) & both).sum())
+
+
+def test_closest_config3_soup_1m(built_lib, orc, parity_report):
+    """Config 3 at 1M triangles: the unit-cube soup and 2^20 of its rays
+    (origins in [-0.5,1.5]^3, uniform directions); the oracle walks the
+    GPU-built tree (byte-equal to the oracle's own build, test_gpu_lbvh)
+    in the reference's order."""
+    import ptgpu_pc_gb300 as pt
+    shapes = scenes.triangle_soup(1 << 20, seed=5)
+    rays = scenes.random_rays(1 << 20, seed=4)
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, 0)
+        ctx.build(abi.ACCEL_BVH)
+        g = ctx.trace_closest(rays)
+        btn, btl = ctx.get_bvh()
+    o = orc.trace_closest(shapes, rays, orc.make_accel(abi.ACCEL_BVH, btn, btl, fast=True))
+    nb, nd = _check(shapes, rays, g, o, parity_report, "closest_config3_soup1m_2^20rays")
+    assert nb > 100_000
 
 
 def test_closest_bvh_soup(built_lib, orc):

@@ -28,6 +28,7 @@ def shim(tmp_path_factory):
     L.shim_check_blocks.argtypes = [ctypes.c_int]
     L.shim_kd_build.argtypes = [vp, ctypes.c_int, vp, vp, vp]
     L.shim_kd_export.argtypes = [vp, ctypes.c_int64, vp]
+    L.shim_kd_export_wide.argtypes = [vp, vp]
     L.shim_read_scene.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp,
                                   ctypes.c_char_p, ctypes.c_int]
     L.shim_scene_get.argtypes = [vp, vp]
@@ -71,12 +72,18 @@ def test_block_fields_short_form(shim):
         assert shim.shim_check_blocks(n) == 0, n
 
 
-@pytest.mark.parametrize("case", ["cornell", "ico2", "ico4", "soup"])
+@pytest.mark.parametrize("case", ["cornell", "ico2", "ico4", "soup", "ico6", "soup100k"])
 def test_kd_build_matches_oracle(case, shim, orc):
+    """The host KD build against the oracle's pointer tree: the int16 heap
+    byte for byte (truncated the reference's way where it overflows, as at the
+    config-2 size, 81,934 shapes) and the 32-bit breadth-first export node by
+    node."""
     shapes = {"cornell": lambda: scenes.cornell_spheres()[0],
               "ico2": lambda: scenes.icosphere_scene(level=2)[0],
               "ico4": lambda: scenes.icosphere_scene(level=4)[0],
-              "soup": lambda: scenes.triangle_soup(3000, seed=9)}[case]()
+              "soup": lambda: scenes.triangle_soup(3000, seed=9),
+              "ico6": lambda: scenes.icosphere_scene(level=6)[0],
+              "soup100k": lambda: scenes.triangle_soup(100_000, seed=29)}[case]()
     md, sz, heap = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
     shim.shim_kd_build(_p(shapes), len(shapes), ctypes.byref(md), ctypes.byref(sz), ctypes.byref(heap))
     kd = orc.KD(shapes)
@@ -89,6 +96,13 @@ def test_kd_build_matches_oracle(case, shim, orc):
         assert st == ost
         assert kng.tobytes() == okng.tobytes()
         assert np.array_equal(kn[: sz.value], okn)
+    from test_gpu_kdtree import _oracle_bfs
+    want = _oracle_bfs(kd)
+    nodes = np.zeros(shim.shim_kd_node_count(), abi.KD_NODE_WIDE)
+    kn = np.zeros(max(sz.value, 1), np.int32)
+    shim.shim_kd_export_wide(_p(nodes), _p(kn))
+    assert nodes.tobytes() == want.tobytes()
+    assert np.array_equal(kn[: sz.value], kd.kn)
 
 
 def test_seeds_match_oracle(shim, orc):
@@ -183,9 +197,11 @@ def test_loader_matches_reference_loader(shim):
     """The reference scene file loaded by the reference's own loader (golden
     fixture) and by this library give the same shapes; needs the reference's
     model files, so it runs only where the reference tree is present."""
-    ref = os.environ.get("PTGPU_REFERENCE_DIR", "/root/reference")
+    ref = os.environ.get("PTGPU_REFERENCE_DIR", "")
+    if not ref:
+        pytest.skip("PTGPU_REFERENCE_DIR is not set (the reference tree is not named)")
     if not os.path.isfile(os.path.join(ref, "scenes", "obj-model.txt")):
-        pytest.skip("reference scene files not present")
+        pytest.skip("reference scene files not found under PTGPU_REFERENCE_DIR")
     z = np.load(os.path.join(HERE, "golden", "obj_model_scene.npz"))
     gold = z["shapes"].view(abi.SHAPE)
     cwd = os.getcwd()

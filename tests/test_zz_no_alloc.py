@@ -28,31 +28,40 @@ def _device_bytes(arr):
     return torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1).copy()).cuda()
 
 
-def _noalloc_bvh(shapes):
-    """Shapes and node arrays in caller-allocated device memory; the call
-    itself goes through the C ABI with the legacy default stream."""
+def _noalloc_bvh(shapes, on_stream=False):
+    """Shapes and node arrays in caller-allocated device memory, each node
+    array followed by one node's worth of guard bytes; the call goes through
+    the C ABI on the legacy default stream, or on a stream of the caller's.
+    Returns the node arrays and whether both guards are untouched."""
     import torch
     import ptgpu_pc_gb300 as pt
     L = pt.lib()
     n = len(shapes)
+    sz = abi.BVH_NODE.itemsize
+    btn_nodes = max(n - 1, 1)
     d_shapes = _device_bytes(shapes)
-    d_btn = torch.full((max(n - 1, 1) * abi.BVH_NODE.itemsize,), 0xAB, dtype=torch.uint8, device="cuda")
-    d_btl = torch.full((n * abi.BVH_NODE.itemsize,), 0xAB, dtype=torch.uint8, device="cuda")
+    d_btn = torch.full(((btn_nodes + 1) * sz,), 0xAB, dtype=torch.uint8, device="cuda")
+    d_btl = torch.full(((n + 1) * sz,), 0xAB, dtype=torch.uint8, device="cuda")
     torch.cuda.synchronize()
+    stream = torch.cuda.Stream() if on_stream else None
+    handle = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
     st = L.ptgpu_build_bvh_noalloc(ctypes.c_void_p(d_shapes.data_ptr()), n,
                                    ctypes.c_void_p(d_btn.data_ptr()), ctypes.c_void_p(d_btl.data_ptr()),
-                                   None)
+                                   handle)
     assert st == 0, L.ptgpu_last_error().decode()
-    btn = d_btn.cpu().numpy()[: (n - 1) * abi.BVH_NODE.itemsize].view(abi.BVH_NODE)
-    btl = d_btl.cpu().numpy().view(abi.BVH_NODE)
-    return btn, btl
+    h_btn, h_btl = d_btn.cpu().numpy(), d_btl.cpu().numpy()
+    guards_ok = bool((h_btn[btn_nodes * sz:] == 0xAB).all() and (h_btl[n * sz:] == 0xAB).all())
+    btn = h_btn[: (n - 1) * sz].view(abi.BVH_NODE)
+    btl = h_btl[: n * sz].view(abi.BVH_NODE)
+    return btn, btl, guards_ok
 
 
-def _check(shapes, light_cnt=0):
+def _check(shapes, light_cnt=0, on_stream=False):
     c_btn, c_btl = _context_bvh(shapes, light_cnt)
-    n_btn, n_btl = _noalloc_bvh(shapes)
+    n_btn, n_btl, guards_ok = _noalloc_bvh(shapes, on_stream)
     assert n_btl.tobytes() == c_btl.tobytes()
     assert n_btn.tobytes() == c_btn.tobytes()
+    assert guards_ok, "bytes written past the node arrays"
 
 
 def test_noalloc_two_calls_in_a_row(built_lib):
@@ -67,6 +76,22 @@ def test_noalloc_icosphere_then_maximum_size(built_lib):
     shapes, light_cnt, _ = scenes.icosphere_scene(level=5)
     _check(shapes, light_cnt)
     _check(scenes.triangle_soup(MAX_SHAPES, seed=22))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3])
+def test_noalloc_smallest_scenes(n, built_lib):
+    """One to three shapes, after a larger build left the shared array
+    stale: the same nodes as the context build, nothing written past them
+    (one shape: btl[0] only, d_btn holds one node)."""
+    _check(scenes.triangle_soup(5000, seed=40))
+    _check(scenes.triangle_soup(n, seed=40 + n))
+
+
+def test_noalloc_on_a_caller_stream(built_lib):
+    """The build enqueued on a stream of the caller's (not the legacy default
+    stream), twice in a row."""
+    _check(scenes.triangle_soup(70_000, seed=44), on_stream=True)
+    _check(scenes.icosphere_scene(level=4)[0], 2, on_stream=True)
 
 
 def test_noalloc_rejects_sizes_beyond_the_array(built_lib):
