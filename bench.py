@@ -12,19 +12,26 @@ Extra keys on the JSON line:
   roofline     the render kernel against HBM, bytes per query after the
                closest-hit model (24 B ray + 8 B hit + 60 B per node visit +
                36 B per primitive test), counts measured by the GPU
-  lbvh         LBVH build of 4,194,304 random triangles: Mtris/s and its HBM
-               roofline at 252 algorithmic bytes per triangle
-  closest_hit  2^24 random rays against the 4M-triangle BVH: Mrays/s
+  treelet      SAH cost, frame time and build time for 0, 1 and 2 rounds
+  ingest       streamed scene ingestion of two OBJ models (1M triangles)
   batched      64 mixed scenes (1k-2M triangles, 128^2-1024^2, 1-64 passes):
                one batch (segmented build, one graph-replayed launch) against
-               the same scenes rendered one by one through contexts
-  served       Poisson request streams over those scenes (10, 100, 1000 req/s,
-               70% of requests on an already requested scene): the server
-               (continuous batching, 120 GB budget, LRU scene cache) against
-               the plain path (first come first served, a context per
-               request); throughput and p50/p99 latency
-  cpu_baseline the oracle port (C, OpenMP, all host threads) on a bounded
-               sample of the same frame
+               the same scenes rendered one by one through contexts, with the
+               per-scene table and the ceiling any schedule could reach
+  served       Poisson request streams over those scenes (10, 30, 100, 300 and
+               1000 req/s, 70% of requests on an already requested scene):
+               the server (continuous batching, 120 GB budget, LRU scene
+               cache) against the plain path (first come first served, a
+               context per request); throughput and p50/p99 latency
+  cpu_baseline the oracle port of the reference's CPU path (C, OpenMP, all
+               host threads) on a bounded sample of the same frame
+  legs         lbvh (4,194,304 random triangles: Mtris/s and its HBM roofline
+               at 252 algorithmic bytes per triangle), lbvh_1m, closest_hit
+               (2^24 random rays against the 4M-triangle BVH), config1 (the
+               9-sphere Cornell box, 256x256, 16 spp, depth 6, no
+               acceleration; also with rr_depth 3), config2_kd (the
+               benchmark frame through the KD tree)
+  summary      the headline figure of every leg, last on the line
 --impl reference times that CPU path alone (rank 0) on the same workload.
 """
 import argparse
@@ -165,62 +172,70 @@ def pinned_copy(torch, arr):
 
 
 class CpuReference:
-    """The oracle port (the reference algorithm restated in C, OpenMP over
-    rows) on a bounded block of pixels at the centre of the same frame: the
-    block is sized once so one timed sample runs for about target_s seconds."""
+    """The oracle port of the reference's CPU path (the reference algorithm
+    restated in C: per pixel RadiancePathTracing with the reference's
+    brute-force IntersectP and its SampleLights scan of the shape list at
+    every diffuse hit; OpenMP over the pixels of a row) on a bounded sample of
+    the same frame: `rows` whole rows spread evenly over the frame, one pass,
+    sized once so that a sample runs for about target_s seconds."""
 
-    def __init__(self, shapes, light_cnt, cam, target_s=10.0, threads=0):
+    def __init__(self, shapes, light_cnt, cam, target_s=10.0, threads=0, w=W, h=H, depth=MAX_DEPTH,
+                 accel="bvh"):
         import oracle
         from ptgpu_pc_gb300 import abi
         oracle.build()
         self.oracle = oracle
         self.shapes, self.lc = shapes, light_cnt
+        self.w, self.h, self.depth = w, h, depth
         c = np.array(cam, abi.CAMERA)
-        c["width"], c["height"] = W, H
+        c["width"], c["height"] = w, h
         self.cam = oracle.update_camera(c)
-        _, btn, btl, _ = oracle.build_bvh(shapes)
-        self.acc = oracle.make_accel(abi.ACCEL_BVH, btn, btl, reference_leafness=True)
-        self.seeds = oracle.make_seeds(1, 2 * W * H)
+        if accel == "bvh":
+            _, btn, btl, _ = oracle.build_bvh(shapes)
+            self.acc = oracle.make_accel(abi.ACCEL_BVH, btn, btl, reference_leafness=True)
+        else:
+            self.acc = oracle.make_accel(abi.ACCEL_NONE)
+        self.accel = accel
+        self.seeds = oracle.make_seeds(1, 2 * w * h)
         self.threads = threads or os.cpu_count() or 1
-        # the port spreads rows over its threads (OpenMP over rows, as DrawBox
-        # does), so a block has at least one row per thread; calibrate on
-        # 8 pixels per row
-        self.rows, self.cols = min(H, self.threads), 8
+        self.rows = 1
         dt = self._run()
-        px_per_s = self.rows * self.cols / max(dt, 1e-6)
-        want = max(self.rows * 8, int(px_per_s * target_s))
-        per_row = -(-want // self.rows)
-        if per_row <= W:
-            self.cols = per_row
-        else:                       # wider than the frame: more rows, a multiple of the threads
-            self.cols = W
-            self.rows = min(H, -(-(-(-want // W)) // self.threads) * self.threads)
+        self.rows = int(max(1, min(h, target_s / max(dt, 1e-6))))
 
-    def _run(self):
-        r0, c0 = H // 2 - self.rows // 2, W // 2 - self.cols // 2
+    def _row_list(self):
+        step = self.h / self.rows
+        return [int(step * (k + 0.5)) for k in range(self.rows)]
+
+    def _run(self, threads=None, cols=None):
         t0 = time.perf_counter()
-        self.oracle.render(self.shapes, self.lc, self.cam, W, H, self.seeds, 1, accel=self.acc,
-                           max_depth=MAX_DEPTH, threads=self.threads, rows=(r0, r0 + self.rows),
-                           cols=(c0, c0 + self.cols))
+        for y in self._row_list():
+            self.oracle.render(self.shapes, self.lc, self.cam, self.w, self.h, self.seeds, 1,
+                               accel=self.acc, max_depth=self.depth, threads=threads or self.threads,
+                               rows=(y, y + 1), cols=cols, reference_cost=True)
         return time.perf_counter() - t0
 
-    def sample(self):
-        dt = self._run()
-        px = self.rows * self.cols
-        desc = ("%dx%d pixel block at the centre of the %dx%d frame, 1 pass, depth %d, BVH built "
-                "by the oracle, brute-force shadow rays as in IntersectP; %.1f s" %
-                (self.cols, self.rows, W, H, MAX_DEPTH, dt))
-        return px / dt / 1e6, self.threads, desc
+    def describe(self, dt, rows=None, cols=None):
+        return ("%d rows x %d pixels spread over the %dx%d frame, 1 pass, depth %d, %s, "
+                "brute-force shadow rays and per-hit emitter scan as in the reference; %.2f s"
+                % (rows or self.rows, cols or self.w, self.w, self.h, self.depth,
+                   "BVH built by the oracle" if self.accel == "bvh" else "no acceleration", dt))
 
-    def sample_one_thread(self):
-        """The same port on one thread, over the middle row of the block."""
-        rows, cols, threads = self.rows, self.cols, self.threads
-        self.rows, self.threads = 1, 1
+    def sample(self):
+        """(Msamples/s, threads, description, seconds) of one timed sample."""
+        dt = self._run()
+        px = self.rows * self.w
+        return px / dt / 1e6, self.threads, self.describe(dt), dt
+
+    def sample_one_thread(self, cols=128):
+        """The same port on one thread, over the first `cols` pixels of the
+        sample's middle row."""
+        rows = self.rows
+        self.rows = 1
         try:
-            dt = self._run()
-            return cols / dt / 1e6, "%dx1 pixel block (the middle row of the block), %.1f s" % (cols, dt)
+            dt = self._run(threads=1, cols=(0, cols))
+            return cols / dt / 1e6, self.describe(dt, rows=1, cols=cols)
         finally:
-            self.rows, self.cols, self.threads = rows, cols, threads
+            self.rows = rows
 
 
 def cpu_model():
@@ -240,47 +255,98 @@ def cpu_model():
 
 
 def run_reference(args, rank, world, pg):
+    """The reference arm: the CPU port of the reference's path on this machine's
+    host cores (all threads), on the same workload, metric and unit as the
+    GPU arm; each step is one bounded sample (whole rows spread over the
+    frame), and ms_per_step is that sample's measured time."""
     from ptgpu_pc_gb300 import scenes
     if rank != 0:
         return
     shapes, lc, cam = scenes.icosphere_scene(level=6)
-    per_step = []
+    per_step, secs = [], []
     desc = ""
     cores = 0
     per = max(1.0, min(args.ref_seconds, 150.0 / (args.warmup + args.steps)))
     ref = CpuReference(shapes, lc, cam, target_s=per)
     for i in range(args.warmup + args.steps):
-        v, cores, desc = ref.sample()
+        v, cores, desc, dt = ref.sample()
         if i >= args.warmup:
             per_step.append(v)
+            secs.append(dt)
     value = float(np.mean(per_step))
-    ms_per_step = W * H * SPP / (value * 1e6) * 1e3
     line = {"metric": "Msamples/s", "value": value, "unit": "Msamples/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced icosphere)",
             "config": {"workload": WORKLOAD, "shapes": int(len(shapes)), "width": W, "height": H,
-                       "spp": SPP, "max_depth": MAX_DEPTH, "accel": "bvh"},
+                       "spp": SPP, "max_depth": MAX_DEPTH, "accel": "bvh",
+                       "step": "one bounded sample of the frame: %d rows x %d pixels x 1 pass"
+                               % (ref.rows, W)},
             "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": cores, "kind": "port",
-                             "sample": desc},
+                             "sample": desc, "cpu": cpu_model()},
             "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def bench_lbvh(pt, abi, scenes, torch, warmup, steps):
-    shapes = scenes.triangle_soup(LBVH_N, seed=3)
-    ctx = pt.Context(8, 8)
-    ctx.set_shapes(shapes, 0)
-    del shapes
-    times = []
-    for i in range(warmup + steps):
-        ctx.build(abi.ACCEL_BVH)
-        if i >= warmup:
-            times.append(ctx.last_build_ms())
-    ms = float(np.mean(times))
-    return ctx, {"metric": "LBVH Mtris/s", "n_tris": LBVH_N, "value": LBVH_N / ms / 1e3,
-                 "unit": "Mtris/s", "ms": ms, "min_ms": float(np.min(times)), "builds": steps}
+def time_frames(ctx, torch, passes, frames, flush=None):
+    """Device time (CUDA events on the context's stream) of `frames` renders
+    of `passes` passes each, after one warm-up frame; L2 flushed before each
+    frame when `flush` (a tensor larger than L2) is given."""
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ctx.reset()
+    ctx.render_async(passes)
+    ctx.synchronize()
+    ms = []
+    for i in range(frames):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+        ctx.reset()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.render_async(passes)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.mean(ms))
+
+
+def bench_config1(pt, abi, scenes, torch, flush, frames=5):
+    """Config 1: the 9-sphere Cornell box, 256x256, 16 passes, depth 6, no
+    acceleration structure (ACCELSTR 0); also with the opt-in throughput
+    Russian roulette from depth 3 (ptgpu_config.rr_depth = 3)."""
+    shapes, lc, cam = scenes.cornell_spheres()
+    w = h = 256
+    out = {"workload": "cornell_spheres_9_256x256_16spp_depth6_none"}
+    for rr in (0, 3):
+        ctx = pt.Context(w, h, accel=abi.ACCEL_NONE, max_depth=6, rr_depth=rr)
+        ctx.set_shapes(shapes, lc)
+        ctx.build(abi.ACCEL_NONE)
+        ctx.set_camera(cam)
+        ctx.set_seeds(pt.make_seeds(1, 2 * w * h))
+        ms = time_frames(ctx, torch, 16, frames, flush)
+        ctx.close()
+        key = "value" if rr == 0 else "rr3_value"
+        out[key] = w * h * 16 / ms / 1e3
+        out["ms" if rr == 0 else "rr3_ms"] = ms
+    out["unit"] = "Msamples/s"
+    return out
+
+
+def bench_config2_kd(pt, abi, shapes, lc, cam, torch, flush, frames=5):
+    """Config 2 through the KD tree (ACCELSTR 2): GPU KD build with the
+    reference topology, then 512x512 x 16 passes at depth 8."""
+    ctx = pt.Context(W, H, accel=abi.ACCEL_KDTREE, max_depth=MAX_DEPTH)
+    ctx.set_shapes(shapes, lc)
+    ctx.build(abi.ACCEL_KDTREE)
+    build_ms = ctx.last_build_ms()
+    ctx.set_camera(cam)
+    ctx.set_seeds(pt.make_seeds(1, 2 * W * H))
+    ms = time_frames(ctx, torch, SPP, frames, flush)
+    ctx.close()
+    return {"workload": WORKLOAD.replace("_bvh", "_kd"), "value": W * H * SPP / ms / 1e3,
+            "unit": "Msamples/s", "ms": ms, "kd_build_ms": build_ms}
 
 
 def sah_cost(btn, btl):
@@ -413,7 +479,7 @@ def served_requests(specs, n_req, rate, seed=5, hit=0.7):
     return out
 
 
-def bench_served(pt, abi, data, specs, rates=(10, 100, 1000), n_req=48):
+def bench_served(pt, abi, data, specs, rates=(10, 30, 100, 300, 1000), n_req=64):
     """Requests arriving at each rate, served with continuous batching (one
     server, 120 GB budget, scenes resident under LRU) and, for comparison,
     by the plain path: one request after another, each building its scene in
@@ -502,8 +568,11 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
     b.close()
     dev_ms = float(np.mean([m[0] for m in ms]))
     frame_wall = float(np.mean([m[1] for m in ms]))
-    # plain: one context per scene, in turn
+    # plain: one context per scene, in turn; per scene also its rate when
+    # its frame fills the GPU (1024x1024, one pass: 8x the lanes the GPU
+    # holds), the best any schedule can do for that scene's samples
     plain_dev_ms, plain_wall = 0.0, 0.0
+    table = []
     for (sh, lc, cam), sp, sd in zip(data, specs, seeds):
         t1 = time.perf_counter()
         ctx = pt.Context(sp["res"], sp["res"], accel=abi.ACCEL_BVH)
@@ -519,9 +588,21 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
         e1.record(stream)
         e1.synchronize()
         ctx.get_pixels()
-        plain_dev_ms += e0.elapsed_time(e1)
+        scene_ms = e0.elapsed_time(e1)
+        plain_dev_ms += scene_ms
         plain_wall += time.perf_counter() - t1
         ctx.close()
+        full = pt.Context(1024, 1024, accel=abi.ACCEL_BVH)
+        full.set_shapes(sh, lc)
+        full.build(abi.ACCEL_BVH, BUILD_FLAGS)
+        full.set_camera(cam)
+        full.set_seeds(pt.make_seeds(5000, 2 * 1024 * 1024))
+        full_ms = time_frames(full, torch, 1, 1)
+        full.close()
+        s_i = sp["res"] * sp["res"] * sp["spp"]
+        table.append({"shapes": int(len(sh)), "res": sp["res"], "spp": sp["spp"], "samples": s_i,
+                      "plain_ms": scene_ms, "plain_msps": s_i / scene_ms / 1e3,
+                      "full_msps": 1024 * 1024 / full_ms / 1e3})
     return data, specs, {"metric": "Msamples/s", "unit": "Msamples/s",
             "workload": "64 scenes, master seed 7: %d shapes, %.1f M samples per frame, depth 6"
                         % (shapes_total, samples / 1e6),
@@ -531,6 +612,12 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
                     "plain_value": samples / plain_wall / 1e6,
                     "per_step": "batched: add + segmented build + render; plain: per scene context, "
                                 "upload, build, render, pixels"},
+            "ceiling": {"speedup": plain_dev_ms / sum(r["samples"] / r["full_msps"] / 1e3 for r in table),
+                        "how": "sum of plain per-scene render ms / sum of (scene samples / that scene's "
+                               "rate on a 1024x1024 one-pass frame, which fills the GPU)",
+                        "small_scene_share": float(sum(r["samples"] for r in table if r["samples"] < 1 << 20))
+                                             / samples},
+            "per_scene": table,
             "render_ms": dev_ms, "plain_render_ms": plain_dev_ms, "build_ms": build_ms,
             "build_wall_s": build_wall, "frames": frames,
             "tuned": {"block": info["block"], "refill": info["refill"], "stack": info["stack"],
@@ -547,6 +634,10 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-extras", action="store_true", help="skip lbvh/closest-hit/cpu legs")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched leg")
+    ap.add_argument("--served-requests", type=int, default=64,
+                    help="requests per arrival rate in the served leg")
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the batched and served legs (the full request sweep)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -558,6 +649,13 @@ def main():
     from ptgpu_pc_gb300 import abi, scenes
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
+    if args.served_only:
+        # the batching leg and the full request sweep on their own (not a
+        # benchmark line: the figures behind profiles/served_sweep.md)
+        data, specs, batched = bench_batched(pt, abi, scenes, torch)
+        served = bench_served(pt, abi, data, specs, n_req=args.served_requests)
+        print(json.dumps({"batched": batched, "served": served}), flush=True)
+        return
 
     shapes, lc, cam = scenes.icosphere_scene(level=6)
     ctx = pt.Context(W, H, accel=abi.ACCEL_BVH, max_depth=MAX_DEPTH, device=local)
@@ -661,14 +759,18 @@ def main():
                                     "shadow_node_visits": sh_v, "shadow_prim_tests": sh_p}},
             "clocks": clk, "wall_s": wall}
     if not args.no_extras:
-        lctx, lb = bench_lbvh(pt, abi, scenes, torch, 2, 5)
-        lb_bytes = 252 * LBVH_N
-        lb_ach = lb_bytes / (lb["ms"] / 1e3) / 1e9
-        lb["roofline"] = {"bound": "hbm", "achieved": lb_ach, "peak": hbm_peak, "unit": "GB/s",
-                          "frac": lb_ach / hbm_peak,
-                          "traffic": ncu_traffic("lbvh_build_soup4m.txt", "traffic_bytes_per_build"),
-                          "peak_kind": peak_kind, "model": "252 B/triangle, whole build"}
-        line["lbvh"] = lb
+        def lbvh_leg(n):
+            lctx, lb = bench_lbvh(pt, abi, scenes, torch, 2, 5, n)
+            lb_ach = 252 * n / (lb["ms"] / 1e3) / 1e9
+            lb["roofline"] = {"bound": "hbm", "achieved": lb_ach, "peak": hbm_peak, "unit": "GB/s",
+                              "frac": lb_ach / hbm_peak,
+                              "traffic": ncu_traffic("lbvh_build_soup4m.txt", "traffic_bytes_per_build")
+                              if n == LBVH_N else None,
+                              "peak_kind": peak_kind, "model": "252 B/triangle, whole build"}
+            return lctx, lb
+        lctx1, lb1 = lbvh_leg(1 << 20)
+        lctx1.close()
+        lctx, lb = lbvh_leg(LBVH_N)
         line["treelet"] = bench_treelet(pt, abi, shapes, lc, cam, torch)
         ch = bench_closest(lctx, torch, scenes, 1, 3)
         ch_ach = ch["model_bytes"] / (ch["ms"] / 1e3) / 1e9
@@ -676,19 +778,39 @@ def main():
                           "frac": ch_ach / hbm_peak, "peak_kind": peak_kind, "kernel": "k_trace_closest_p",
                           "model": "per ray 32 B + 60 B/node visit + 36 B/prim test, GPU-counted; "
                                    "served by L1/L2 (profiles/k_trace_closest_p_soup1m_4mrays.txt)"}
-        line["closest_hit"] = ch
         lctx.close()
         line["ingest"] = bench_ingest(pt, abi, scenes)
+        c1 = bench_config1(pt, abi, scenes, torch, flush)
+        kd = bench_config2_kd(pt, abi, shapes, lc, cam, torch, flush)
         if not args.no_batched:
             data, specs, line["batched"] = bench_batched(pt, abi, scenes, torch)
-            line["served"] = bench_served(pt, abi, data, specs)
+            line["served"] = bench_served(pt, abi, data, specs, n_req=args.served_requests)
         if rank == 0:
             cref = CpuReference(shapes, lc, cam, target_s=args.ref_seconds)
-            v, cores, desc = cref.sample()
+            v, cores, desc, _ = cref.sample()
             v1, desc1 = cref.sample_one_thread()
             line["cpu_baseline"] = {"value": v, "unit": "Msamples/s", "cores": cores,
                                     "kind": "port", "sample": desc, "cpu": cpu_model(),
                                     "one_thread": {"value": v1, "sample": desc1}}
+        # the figures of every leg, last on the line
+        summ = {"lbvh_4m": {"ms": lb["ms"], "mtris_s": lb["value"], "frac": lb["roofline"]["frac"],
+                            "achieved_gbs": lb["roofline"]["achieved"],
+                            "traffic": lb["roofline"]["traffic"]},
+                "lbvh_1m": {"ms": lb1["ms"], "mtris_s": lb1["value"], "frac": lb1["roofline"]["frac"]},
+                "closest_hit_4m_2^24": {"mrays_s": ch["value"], "ms": ch["ms"],
+                                        "bytes_model_frac": ch["roofline"]["frac"]},
+                "config1_spheres": {"msps": c1["value"], "rr3_msps": c1["rr3_value"]},
+                "config2_kd": {"msps": kd["value"], "kd_build_ms": kd["kd_build_ms"]},
+                "config2_bvh": {"msps": value, "e2e_msps": e2e_value, "scene_build_ms": build_ms}}
+        if "batched" in line:
+            b = line["batched"]
+            summ["batched"] = {"msps": b["value"], "plain_msps": b["plain_value"],
+                               "speedup": b["speedup_vs_plain"], "ceiling": b["ceiling"]["speedup"]}
+            summ["served"] = [{"rate": r["rate_per_s"], "msps": r["value"], "plain_msps": r["plain_value"],
+                               "p50": r["p50_ms"], "p99": r["p99_ms"], "plain_p50": r["plain_p50_ms"],
+                               "plain_p99": r["plain_p99_ms"]} for r in line["served"]]
+        line["legs"] = {"closest_hit": ch, "config1": c1, "config2_kd": kd, "lbvh_1m": lb1, "lbvh": lb}
+        line["summary"] = summ
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -119,7 +119,13 @@ typedef struct {
     int32_t width, height; /* image size; sets camera.width/height              */
     int32_t block_size;    /* render block size; 0 = default                    */
     int32_t flags;         /* PTGPU_FLAG_*                                       */
-    int32_t reserved;
+    int32_t rr_depth;      /* 0: paths end only at max_depth (the reference);
+                              d > 0: throughput Russian roulette from the hit
+                              at depth d (0-based) on: a path continues with
+                              probability p = min(max(throughput), 1) and its
+                              throughput is divided by p (one random per
+                              roll, drawn after the bounce's).  Lane tracer
+                              only: with PTGPU_FLAG_WAVEFRONT, E_INVAL.       */
     void   *stream;        /* optional cudaStream_t; NULL = context-owned stream */
 } ptgpu_config;
 

@@ -85,6 +85,8 @@ def lib():
         L.orc_kd_heap.argtypes = [ctypes.POINTER(KdTree), vp, i32, vp]
         L.orc_to_int.restype = u32
         L.orc_set_portable_trig.argtypes = [i32]
+        L.orc_set_rr_depth.argtypes = [i32]
+        L.orc_set_reference_cost.argtypes = [i32]
         L.orc_to_int.argtypes = [f32]
         _lib = L
     return _lib
@@ -226,10 +228,15 @@ def shadow_batch(shapes, rays, maxt, accel=None, threads=0):
 
 def render(shapes, light_cnt, cam, w, h, seeds, passes, accel=None, max_depth=6,
            arg_order_rtl=False, colors=None, start_sample=0, threads=0, rows=None,
-           portable_trig=False, cols=None):
+           portable_trig=False, cols=None, rr_depth=0, reference_cost=False):
     """Runs `passes` RadianceGPU passes; returns (colors, pixels, seeds).
-    portable_trig selects the GPU library's own sin/cos instead of libm."""
+    portable_trig selects the GPU library's own sin/cos instead of libm;
+    rr_depth > 0 adds the opt-in throughput Russian roulette;
+    reference_cost rescans the shapes for emitters at every diffuse hit, as
+    the reference does (same result, the reference's cost)."""
     lib().orc_set_portable_trig(1 if portable_trig else 0)
+    lib().orc_set_rr_depth(int(rr_depth))
+    lib().orc_set_reference_cost(1 if reference_cost else 0)
     shapes = abi.as_struct(shapes, abi.SHAPE)
     cam = np.array(cam, abi.CAMERA).reshape(1)
     seeds = np.array(seeds, np.uint32, copy=True)

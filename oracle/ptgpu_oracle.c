@@ -468,6 +468,30 @@ static void sample_lights(const ptgpu_shape *shapes, uint32_t n, const uint32_t 
     }
 }
 
+/* Optional throughput Russian roulette, off by default (the reference has
+ * none: its paths end only past MAX_DEPTH, rendering_kernel.cl:797-801).
+ * With rr_depth = d > 0, a path about to continue past its hit at depth
+ * `depth` >= d (and within max_depth) draws one random u and ends when
+ * u >= p, p = min(max(throughput), 1); otherwise its throughput is divided by
+ * p.  The GPU library's ptgpu_config.rr_depth does the same. */
+static int g_rr_depth = 0;
+void orc_set_rr_depth(int d) { g_rr_depth = d; }
+
+/* 1: every diffuse hit scans the shape list for its emitters again, as the
+ * reference's SampleLights does (rendering_kernel.cl:403-407,
+ * geomfunc.h:383) -- the same lights in the same order, at the reference's
+ * cost; for the timed CPU baseline.  0: the list collected once per pass. */
+static int g_reference_cost = 0;
+void orc_set_reference_cost(int on) { g_reference_cost = on; }
+static int rr_stop(unsigned depth, int max_depth, ptgpu_vec *tp, uint32_t *s0, uint32_t *s1) {
+    if (g_rr_depth <= 0 || (int)depth < g_rr_depth || (int)depth + 1 > max_depth) return 0;
+    const float u = orc_get_random(s0, s1);
+    const float p = fminf(fmaxf(tp->x, fmaxf(tp->y, tp->z)), 1.f);
+    if (!(u < p)) return 1;
+    *tp = vsmul(1.f / p, *tp);
+    return 0;
+}
+
 /* RadianceOnePathTracing + RadiancePathTracing (rendering_kernel.cl:495-820) */
 static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *lights,
                      uint32_t n_lights, const orc_accel *acc, int max_depth, int rtl,
@@ -519,7 +543,15 @@ static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *ligh
             specular = 0;
             tp = vmul(tp, col);
             ptgpu_vec ld;
-            sample_lights(shapes, n, lights, n_lights, acc, rtl, s0, s1, hp, nl, &ld);
+            if (g_reference_cost) {
+                uint32_t again[8];
+                if (n_lights <= 8 && collect_lights(shapes, n, n_lights, again) == n_lights)
+                    sample_lights(shapes, n, again, n_lights, acc, rtl, s0, s1, hp, nl, &ld);
+                else
+                    sample_lights(shapes, n, lights, n_lights, acc, rtl, s0, s1, hp, nl, &ld);
+            } else {
+                sample_lights(shapes, n, lights, n_lights, acc, rtl, s0, s1, hp, nl, &ld);
+            }
             ld = vmul(ld, tp);
             rad = vadd(rad, ld);
             float r1 = 2.f * ORC_PI * orc_get_random(s0, s1);
@@ -537,11 +569,13 @@ static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *ligh
             w = vsmul(sqrtf(1.f - r2), w);
             nd = vadd(nd, w);
             ray.o = hp; ray.d = nd;
+            if (rr_stop(depth, max_depth, &tp, s0, s1)) break;
         } else if (s->refl == PTGPU_SPEC) {
             specular = 1;
             ptgpu_vec nd = vsub(ray.d, vsmul(2.f * vdot(normal, ray.d), normal));
             tp = vmul(tp, col);
             ray.o = hp; ray.d = nd;
+            if (rr_stop(depth, max_depth, &tp, s0, s1)) break;
         } else {
             specular = 1;
             ptgpu_vec refl_d = vsub(ray.d, vsmul(2.f * vdot(normal, ray.d), normal));
@@ -553,6 +587,7 @@ static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *ligh
             if (cos2t < 0.f) {
                 tp = vmul(tp, col);
                 ray.o = hp; ray.d = refl_d;
+                if (rr_stop(depth, max_depth, &tp, s0, s1)) break;
                 continue;
             }
             float kk = (float)(into ? 1 : -1) * (ddn * nnt + sqrtf(cos2t));
@@ -575,6 +610,7 @@ static void radiance(const ptgpu_shape *shapes, uint32_t n, const uint32_t *ligh
                 tp = vmul(tp, col);
                 ray.o = hp; ray.d = tdir;
             }
+            if (rr_stop(depth, max_depth, &tp, s0, s1)) break;
         }
     }
     *result = rad;

@@ -92,6 +92,12 @@ uint32_t orc_to_int(float x);
 /* 0: sin/cos from libm (as the reference source compiled here); 1: the
  * library's own deterministic sin/cos (as the GPU computes them) */
 void  orc_set_portable_trig(int on);
+/* 0: no throughput Russian roulette (the reference); d > 0: roulette from
+ * the hit at depth d on (see rr_stop in ptgpu_oracle.c) */
+void  orc_set_rr_depth(int d);
+/* 1: SampleLights rescans the shapes for emitters at every diffuse hit, as
+ * the reference does (the timed CPU baseline); 0: once per pass */
+void  orc_set_reference_cost(int on);
 
 /* LBVH */
 void  orc_lbvh_morton(ptgpu_shape *shapes, uint32_t n);

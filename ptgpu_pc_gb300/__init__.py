@@ -140,11 +140,12 @@ class Context:
     """One ptgpu_ctx: a scene, its acceleration structure and a frame."""
 
     def __init__(self, width, height, accel=abi.ACCEL_BVH, max_depth=0, device=0,
-                 block_size=0, flags=0, stream=None):
+                 block_size=0, flags=0, stream=None, rr_depth=0):
         cfg = np.zeros(1, abi.CONFIG)
         cfg["device"], cfg["accel"], cfg["max_depth"] = device, accel, max_depth
         cfg["width"], cfg["height"] = width, height
         cfg["block_size"], cfg["flags"] = block_size, flags
+        cfg["rr_depth"] = rr_depth
         cfg["stream"] = int(stream or 0)
         self._h = ctypes.c_void_p()
         self.width, self.height = width, height

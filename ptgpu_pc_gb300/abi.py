@@ -58,7 +58,7 @@ KD_NODE_WIDE = np.dtype({
 
 CONFIG = np.dtype({
     "names": ["device", "accel", "max_depth", "width", "height", "block_size",
-              "flags", "reserved", "stream"],
+              "flags", "rr_depth", "stream"],
     "formats": ["<i4"] * 8 + ["<u8"],
     "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32],
     "itemsize": 40,

@@ -126,6 +126,7 @@ struct ptgpu_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_build_ms = 0.f;
     int rtl = 0;
+    int rr_depth = 0;     // ptgpu_config.rr_depth
 };
 
 static TraceView make_view(ptgpu_ctx *c) {
@@ -188,6 +189,9 @@ int ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out) {
         return fail(PTGPU_E_INVAL, "width and height must be positive");
     if (cfg->accel < 0 || cfg->accel > 2) return fail(PTGPU_E_INVAL, "accel must be 0, 1 or 2");
     if (cfg->max_depth < 0 || cfg->max_depth > 1024) return fail(PTGPU_E_INVAL, "bad max_depth");
+    if (cfg->rr_depth < 0) return fail(PTGPU_E_INVAL, "rr_depth must be >= 0");
+    if (cfg->rr_depth > 0 && (cfg->flags & PTGPU_FLAG_WAVEFRONT))
+        return fail(PTGPU_E_INVAL, "rr_depth applies to the lane tracer, not PTGPU_FLAG_WAVEFRONT");
     *out = nullptr;
     ptgpu_ctx *c = new ptgpu_ctx();
     c->device = cfg->device;
@@ -196,6 +200,7 @@ int ptgpu_create(const ptgpu_config *cfg, ptgpu_ctx **out) {
     c->block = cfg->block_size > 0 ? cfg->block_size : 128;
     c->flags = cfg->flags;
     c->rtl = (cfg->flags & PTGPU_FLAG_ARGS_RTL) ? 1 : 0;
+    c->rr_depth = cfg->rr_depth;
     c->wide = (cfg->flags & PTGPU_FLAG_WIDE_TRAVERSAL) ? true : false;
     c->w = cfg->width;
     c->h = cfg->height;
@@ -698,6 +703,7 @@ static int enqueue_render(ptgpu_ctx *c, uint32_t passes, unsigned long long *sta
     a.passes = (int32_t)passes;
     a.max_depth = c->max_depth;
     a.rtl = c->rtl;
+    a.rr_depth = c->rr_depth;
     a.colors = c->d_colors.as<ptgpu_vec>();
     a.pixels = c->d_pixels.as<uint32_t>();
     a.seeds = c->d_seeds.as<uint32_t>();

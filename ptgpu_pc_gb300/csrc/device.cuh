@@ -163,6 +163,39 @@ __device__ __forceinline__ float f4get(const float4 &v, int k) {
 }
 __device__ __forceinline__ int i4get(const float4 &v, int k) { return __float_as_int(f4get(v, k)); }
 
+// ---------------------------------------------------------------------------
+// Traversal stacks.  LocalStack keeps all of a lane's entries in a local
+// array.  ShortStack keeps the bottom SHORT entries in shared memory and only
+// the deeper ones in a local array: entry j of lane t sits at
+// s[j * LANES + t], so a lane always uses its own bank (LANES is a multiple of
+// 32) whatever depth the other lanes are at, and a traversal that stays
+// within SHORT entries -- nearly every one in a front-to-back walk -- never
+// touches local memory.  Both hold at most STACK entries.
+// ---------------------------------------------------------------------------
+template <int STACK>
+struct LocalStack {
+    int loc[STACK];
+    __device__ __forceinline__ void put(int i, int v) { loc[i] = v; }
+    __device__ __forceinline__ int get(int i) const { return loc[i]; }
+};
+
+template <int STACK, int SHORT, int LANES>
+struct ShortStack {
+    static_assert(SHORT > 0 && SHORT < STACK && LANES % 32 == 0, "short stack shape");
+    int *sh;                        // &shared[0][lane of the block]
+    int loc[STACK - SHORT];
+    __device__ __forceinline__ void put(int i, int v) {
+        if (i < SHORT) sh[i * LANES] = v;
+        else loc[i - SHORT] = v;
+    }
+    __device__ __forceinline__ int get(int i) const { return i < SHORT ? sh[i * LANES] : loc[i - SHORT]; }
+};
+
+// entries of a lane's stack kept in shared memory (0: all in local memory)
+#ifndef PTGPU_SHORT_STACK
+#define PTGPU_SHORT_STACK 16
+#endif
+
 // A query in flight: the ray, the best hit so far and the traversal
 // position (current item and stack depth; the stack itself is the caller's).
 // trav_begin sets it up, trav_step advances it by one item, so a kernel can
@@ -251,8 +284,8 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f
 #ifndef PTGPU_TRAV_FUSE
 #define PTGPU_TRAV_FUSE 1
 #endif
-template <bool WIDE, bool COUNT, int STACK = kStackSize>
-__device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *stack, Counts *cnt) {
+template <bool WIDE, bool COUNT, int STACK = kStackSize, class Stack>
+__device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, Stack &stack, Counts *cnt) {
     if (q.ccnt > 0) {
         for (int k = q.cur; k < q.cur + q.ccnt; ++k) {
             if (q.any && __ldg(&tv.prim_id[k]) == q.skip) continue;
@@ -271,8 +304,8 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
             }
         }
         if (q.sp == 0) return true;
-        int e = stack[--q.sp];
-        if (e < 0) { q.cur = ~e; q.ccnt = stack[--q.sp]; }
+        int e = stack.get(--q.sp);
+        if (e < 0) { q.cur = ~e; q.ccnt = stack.get(--q.sp); }
         else { q.cur = e; q.ccnt = 0; }
         // a node popped after a leaf is visited in the same step, so lanes
         // at a leaf and lanes at a node share the node half of the step
@@ -314,12 +347,12 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
             }
         }
         for (int a = ni - 1; a >= 0; --a) {
-            if (q.sp < STACK) stack[q.sp++] = iref[a];
+            if (q.sp < STACK) stack.put(q.sp++, iref[a]);
             else if (tv.error_flags) atomicOr(tv.error_flags, 1);
         }
         // leaves go on the stack as negative entries, tested before the nodes
         for (int a = nl - 1; a >= 0; --a) {
-            if (q.sp + 1 < STACK) { stack[q.sp++] = lcnt[a]; stack[q.sp++] = ~lref[a]; }
+            if (q.sp + 1 < STACK) { stack.put(q.sp++, lcnt[a]); stack.put(q.sp++, ~lref[a]); }
             else if (tv.error_flags) atomicOr(tv.error_flags, 1);
         }
     } else {
@@ -338,8 +371,8 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
             int fr = lfirst ? q3.y : q3.x, fc = lfirst ? q3.w : q3.z;
             int nr = lfirst ? q3.x : q3.y, nc = lfirst ? q3.z : q3.w;
             if (q.sp + 1 < STACK) {
-                if (fc > 0) { stack[q.sp++] = fc; stack[q.sp++] = ~fr; }
-                else stack[q.sp++] = fr;
+                if (fc > 0) { stack.put(q.sp++, fc); stack.put(q.sp++, ~fr); }
+                else stack.put(q.sp++, fr);
             } else if (tv.error_flags) atomicOr(tv.error_flags, 1);
             q.cur = nr; q.ccnt = nc;
             return false;
@@ -348,8 +381,8 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, int *sta
         if (rh) { q.cur = q3.y; q.ccnt = q3.w; return false; }
     }
     if (q.sp == 0) return true;
-    int e = stack[--q.sp];
-    if (e < 0) { q.cur = ~e; q.ccnt = stack[--q.sp]; }
+    int e = stack.get(--q.sp);
+    if (e < 0) { q.cur = ~e; q.ccnt = stack.get(--q.sp); }
     else { q.cur = e; q.ccnt = 0; }
     return false;
 }
@@ -360,7 +393,7 @@ template <bool WIDE, bool COUNT>
 __device__ __forceinline__ int trace_query(const TraceView &tv, f3 o, f3 d, bool any, float maxt,
                                            float &t, int &prim, Counts *cnt) {
     Trav q;
-    int stack[kStackSize];
+    LocalStack<kStackSize> stack;
     if (!trav_begin<COUNT>(tv, q, o, d, any, maxt, cnt))
         while (!trav_step<WIDE, COUNT>(tv, q, stack, cnt)) {}
     t = any ? kInfT : q.tb;

@@ -172,6 +172,63 @@ __global__ void k_init_build(BuildState *st, uint4 *__restrict__ status, size_t 
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < arrival_words; i += stride) arrivals[i] = 0u;
 }
 
+// ---------------------------------------------------------------------------
+// L2 residency of the bound records.  k_emit gathers each leaf's 32-byte
+// bound record in sorted order, i.e. at random; those records are written by
+// k_centroid_bounds four radix passes earlier.  Data that only streams
+// through L2 in between can be read and written with the streaming cache
+// operator (.cs: evict first), so that the bound records are what L2 keeps
+// until the gather.  PTGPU_L2_HINTS selects where, one bit per site:
+//   1  the radix passes' key and value loads and stores
+//   2  k_centroid_bounds' vertex copies
+//   4  k_emit's index and bound-record loads (their last use)
+//   8  k_emit's node-record stores
+//  16  the bound records stored and re-read with an evict-last L2 policy
+// ---------------------------------------------------------------------------
+#ifndef PTGPU_L2_HINTS
+#define PTGPU_L2_HINTS 0
+#endif
+constexpr int kL2Sort = 1, kL2Verts = 2, kL2Gather = 4, kL2Nodes = 8, kL2BoundsLast = 16;
+__host__ __device__ constexpr bool l2_hint(int bit) { return (PTGPU_L2_HINTS & bit) != 0; }
+
+template <int BIT> __device__ __forceinline__ uint32_t ld_hint_u32(const uint32_t *a) {
+    if constexpr (l2_hint(BIT)) return __ldcs(a);
+    else return __ldg(a);
+}
+template <int BIT> __device__ __forceinline__ int32_t ld_hint_s32(const int32_t *a) {
+    if constexpr (l2_hint(BIT)) return __ldcs(a);
+    else return __ldg(a);
+}
+template <int BIT> __device__ __forceinline__ float4 ld_hint_f4(const float4 *a) {
+    if constexpr (l2_hint(BIT)) return __ldcs(a);
+    else return __ldg(a);
+}
+template <int BIT> __device__ __forceinline__ void st_hint_u32(uint32_t *a, uint32_t v) {
+    if constexpr (l2_hint(BIT)) __stcs(a, v);
+    else *a = v;
+}
+template <int BIT> __device__ __forceinline__ void st_hint_u4(uint4 *a, uint4 v) {
+    if constexpr (l2_hint(BIT)) __stcs(a, v);
+    else *a = v;
+}
+// evict-last L2 policy accesses of the bound records (bit 16)
+__device__ __forceinline__ void st_last_f4(float4 *a, float4 v) {
+    asm volatile("{\n\t.reg .b64 pol;\n\t"
+                 "createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
+                 "st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, pol;\n\t}" ::"l"(a),
+                 "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+__device__ __forceinline__ float4 ld_last_f4(const float4 *a) {
+    float4 v;
+    asm("{\n\t.reg .b64 pol;\n\t"
+        "createpolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
+        "ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], pol;\n\t}"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(a));
+    return v;
+}
+
 // Centroid bounds, and each shape's bound stored as one aligned 32-byte
 // record for the later kernels (the emission kernel gathers it in sorted
 // order: one sector per leaf instead of a 36-byte vertex triple).
@@ -180,8 +237,13 @@ __device__ __forceinline__ void centroid_shape(const float *__restrict__ v, bool
                                                float4 *__restrict__ rec, float lo[3], float hi[3]) {
     float b[6];
     shape_bound(v, 0, tri, b);
-    rec[0] = make_float4(b[0], b[1], b[2], b[3]);
-    rec[1] = make_float4(b[4], b[5], 0.f, 0.f);
+    if constexpr (l2_hint(kL2BoundsLast)) {
+        st_last_f4(rec, make_float4(b[0], b[1], b[2], b[3]));
+        st_last_f4(rec + 1, make_float4(b[4], b[5], 0.f, 0.f));
+    } else {
+        rec[0] = make_float4(b[0], b[1], b[2], b[3]);
+        rec[1] = make_float4(b[4], b[5], 0.f, 0.f);
+    }
     const float c[3] = {tri ? (b[0] + b[1]) / 2.0f : v[0], tri ? (b[2] + b[3]) / 2.0f : v[1],
                         tri ? (b[4] + b[5]) / 2.0f : v[2]};
     for (int a = 0; a < 3; ++a) {
@@ -195,10 +257,19 @@ __device__ __forceinline__ void centroid_shape(const float *__restrict__ v, bool
 #ifndef PTGPU_CENTROID_PIPE
 #define PTGPU_CENTROID_PIPE 1
 #endif
+
 // 16-byte global -> shared copies that complete asynchronously (L2 only)
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
     const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+    if constexpr (l2_hint(kL2Verts)) {   // vertices are read once: evict first
+        asm volatile("{\n\t.reg .b64 pol;\n\t"
+                     "createpolicy.fractional.L2::evict_first.b64 pol, 1.0;\n\t"
+                     "cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, pol;\n\t}" ::"r"(d),
+                     "l"(gmem_src)
+                     : "memory");
+    } else {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+    }
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
@@ -345,8 +416,13 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
         if (blk >= 0 && i < n) {
             tri = all_tri || type[i] == PTGPU_TRIANGLE;
             if (tri) {
-                r0 = aabbs[2 * (size_t)i];
-                r1 = aabbs[2 * (size_t)i + 1];
+                if constexpr (l2_hint(kL2BoundsLast)) {   // read again by k_emit: keep
+                    r0 = ld_last_f4(aabbs + 2 * (size_t)i);
+                    r1 = ld_last_f4(aabbs + 2 * (size_t)i + 1);
+                } else {
+                    r0 = aabbs[2 * (size_t)i];
+                    r1 = aabbs[2 * (size_t)i + 1];
+                }
             } else {
                 const f3 c = shape_centroid(verts, i, false);
                 r0 = make_float4(c.x, c.y, c.z, 0.f);
@@ -750,10 +826,10 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
         const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
         const bool valid = idx < n;
         if constexpr (SEG) {   // seg_off is in shared memory after the barrier above
-            const int32_t v = valid ? vals_in[idx] : -1;
+            const int32_t v = valid ? ld_hint_s32<kL2Sort>(vals_in + idx) : -1;
             key[j] = v >= 0 ? segment_of(sm.seg_off, n_segs, v) : 0xffffffffu;
         } else {
-            key[j] = valid ? keys_in[idx] : 0xffffffffu;
+            key[j] = valid ? ld_hint_u32<kL2Sort>(keys_in + idx) : 0xffffffffu;
         }
     }
 #if PTGPU_SORT_PREFETCH
@@ -809,7 +885,7 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
             uint32_t pos = sm.digit_start[dig] + sm.warp_hist[w][dig] + rank[j];
             sm.u.st.keys[pos] = key[j];
             const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
-            sm.u.st.vals[pos] = FIRST ? (int32_t)idx : vals_in[idx];
+            sm.u.st.vals[pos] = FIRST ? (int32_t)idx : ld_hint_s32<kL2Sort>(vals_in + idx);
         }
     }
     __syncthreads();
@@ -820,8 +896,8 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
         uint32_t dig = (k >> shift) & 255u;
         uint32_t dest = sm.tile_excl[dig] + (uint32_t)i;
         if (dest < (uint32_t)n) {
-            if (!LAST) keys_out[dest] = k;
-            vals_out[dest] = sm.u.st.vals[i];
+            if (!LAST) st_hint_u32<kL2Sort>(keys_out + dest, k);
+            st_hint_u32<kL2Sort>(reinterpret_cast<uint32_t *>(vals_out) + dest, (uint32_t)sm.u.st.vals[i]);
         }
     }
 }
@@ -1089,9 +1165,9 @@ static_assert(kEmitLeaves == kLeafThreads, "one leaf per thread");
 __device__ __forceinline__ void gather_bound(const float4 *__restrict__ aabbs,
                                              const int32_t *__restrict__ sorted, int k, int n,
                                              int &sh, float4 &q0, float4 &q1) {
-    sh = min(max(__ldg(sorted + k), 0), n - 1);                 // in bounds even after a failed sort
-    q0 = __ldg(aabbs + 2 * (size_t)sh);
-    q1 = __ldg(aabbs + 2 * (size_t)sh + 1);
+    sh = min(max(ld_hint_s32<kL2Gather>(sorted + k), 0), n - 1);   // in bounds even after a failed sort
+    q0 = ld_hint_f4<kL2Gather>(aabbs + 2 * (size_t)sh);
+    q1 = ld_hint_f4<kL2Gather>(aabbs + 2 * (size_t)sh + 1);
 }
 
 // stages the record of the block at `level` starting at leaf T0 + l0 into
@@ -1159,8 +1235,8 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
             uint32_t *dst = reinterpret_cast<uint32_t *>(btl + k0);
             const int words = cnt * kRecWords, chunks = words >> 2;
             for (int q = tid; q < chunks; q += kLeafThreads)
-                reinterpret_cast<uint4 *>(dst)[q] = reinterpret_cast<const uint4 *>(rec)[q];
-            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) dst[q] = rec[q];
+                st_hint_u4<kL2Nodes>(reinterpret_cast<uint4 *>(dst) + q, reinterpret_cast<const uint4 *>(rec)[q]);
+            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) st_hint_u32<kL2Nodes>(dst + q, rec[q]);
         }
         __syncthreads();                            // staging buffer free
         // ---- the warp's level 1-5 nodes, one per lane (lane 31 idle)
@@ -1201,8 +1277,8 @@ __global__ void __launch_bounds__(kLeafThreads, PTGPU_EMIT_MINBLOCKS) k_emit(con
             const int last = min(kEmitLeaves, n - 1 - k0);     // internal indices < n-1
             const int words = max(last, 0) * kRecWords, chunks = words >> 2;
             for (int q = tid; q < chunks; q += kLeafThreads)
-                reinterpret_cast<uint4 *>(dst)[q] = reinterpret_cast<const uint4 *>(rec)[q];
-            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) dst[q] = rec[q];
+                st_hint_u4<kL2Nodes>(reinterpret_cast<uint4 *>(dst) + q, reinterpret_cast<const uint4 *>(rec)[q]);
+            for (int q = 4 * chunks + tid; q < words; q += kLeafThreads) st_hint_u32<kL2Nodes>(dst + q, rec[q]);
         }
         __syncthreads();                            // rec and the slots are reused
     }

@@ -120,6 +120,7 @@ struct RenderArgs {
     int32_t start_sample, passes;
     int32_t max_depth;
     int32_t rtl;                // evaluate light-sample random pairs right-to-left
+    int32_t rr_depth;           // > 0: throughput Russian roulette from that hit depth on
     ptgpu_vec *colors;          // W*H, row-flipped (RadianceGPU)
     uint32_t *pixels;           // W*H RGBA8
     uint32_t *seeds;            // 2*W*H

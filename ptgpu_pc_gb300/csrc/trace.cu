@@ -122,7 +122,15 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
     q.any = 0; q.hit = 0; q.skip = -1;
-    int stack[STACK];
+#if PTGPU_SHORT_STACK > 0
+    // the bottom of each lane's traversal stack in shared memory, the rest in
+    // local memory (ShortStack)
+    __shared__ int s_stack[PTGPU_SHORT_STACK][128];
+    ShortStack<STACK, PTGPU_SHORT_STACK, 128> stack;
+    stack.sh = &s_stack[0][threadIdx.x];
+#else
+    LocalStack<STACK> stack;
+#endif
     bool trav = false;   // a query in flight
     bool fin = false;    // an answered query not yet consumed
     Counts cnt[3] = {{0, 0}, {0, 0}, {0, 0}};
@@ -136,6 +144,20 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     auto n_lights = [&]() { return BATCH ? __ldg(&S().n_lights) : a.n_lights; };
     auto start_sample = [&]() { return BATCH ? __ldg(&S().start_sample) : a.start_sample; };
     auto passes = [&]() { return BATCH ? __ldg(&S().passes) : a.passes; };
+
+    // Optional throughput Russian roulette (RenderArgs::rr_depth > 0, single
+    // scene only): called when a path is about to continue past a hit, with
+    // `depth` already the next segment's; from the hit at depth rr_depth on
+    // it draws one random and ends the path with probability 1 - p,
+    // p = min(max(throughput), 1), or divides the throughput by p.
+    auto rr_stop = [&]() -> bool {
+        if (BATCH || a.rr_depth <= 0 || depth - 1 < a.rr_depth) return false;
+        const float u = get_random(s0, s1);
+        const float pr = fminf(fmaxf(tp.x, fmaxf(tp.y, tp.z)), 1.f);
+        if (!(u < pr)) return true;
+        tp = smul3(1.f / pr, tp);
+        return false;
+    };
 
     // starts a query; an immediately answered one is consumed like any other
     auto start = [&](f3 o, f3 d, bool any, float maxt) {
@@ -285,7 +307,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                     f3 nd = add3(u, v);
                     w = smul3(sqrtf(1.f - r2), w);
                     nd = add3(nd, w);
-                    if (++depth > max_depth()) {
+                    if (++depth > max_depth() || rr_stop()) {
                         state = -1;   // pass finished
                     } else {
                         state = ST_EXT;
@@ -401,7 +423,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
                             }
                         }
                     }
-                    if (++depth > max_depth()) {
+                    if (++depth > max_depth() || rr_stop()) {
                         state = -1;
                     } else {
                         if (COUNT) cnt[2].p++;
@@ -620,7 +642,13 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
     const TraceRoot root = view_root(tv);
     Trav q;
     q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0; q.skip = -1;
-    int stack[kStackSize];
+#if PTGPU_SHORT_STACK > 0
+    __shared__ int s_stack[PTGPU_SHORT_STACK][128];
+    ShortStack<kStackSize, PTGPU_SHORT_STACK, 128> stack;
+    stack.sh = &s_stack[0][threadIdx.x];
+#else
+    LocalStack<kStackSize> stack;
+#endif
     int ray = -1;
     bool trav = false, fin = false, done = false;
     for (;;) {

@@ -189,3 +189,44 @@ def test_config2_icosphere_rows(accel, config2, built_lib, orc, parity_report):
     assert rel_pt < RMSE_TOL
     assert same_pt > 0.999
     assert (g_sd[seed_idx] == p_sd[seed_idx]).mean() > 0.999
+
+
+# ---------------------------------------------------------------------------
+# config 1 with the opt-in throughput Russian roulette (rr_depth = 3)
+# ---------------------------------------------------------------------------
+def test_config1_russian_roulette_option(config1, built_lib, orc, parity_report):
+    """Config 1's "Russian roulette after depth 3": ptgpu_config.rr_depth = 3
+    on the GPU and the same roulette in the oracle consume the same randoms
+    and give the same image (portable sine/cosine: bit for bit); the
+    reference itself has no such roulette, so rr_depth = 0 stays the
+    default."""
+    import ptgpu_pc_gb300 as pt
+    c = config1
+    w, h = C1["w"], C1["h"]
+    with pt.Context(w, h, accel=abi.ACCEL_NONE, max_depth=C1["depth"], flags=abi.FLAG_ARGS_RTL,
+                    rr_depth=3) as ctx:
+        ctx.set_shapes(c["shapes"], c["lc"])
+        ctx.build(abi.ACCEL_NONE)
+        ctx.set_camera(c["cam"])
+        ctx.set_seeds(c["seeds"])
+        ctx.draw_frame(C1["spp"])
+        g_col, g_sd = ctx.get_colors(), ctx.get_seeds()
+    ocam = _cam(c["cam"], w, h, orc)
+    o_col, _, o_sd = orc.render(c["shapes"], c["lc"], ocam, w, h, c["seeds"], C1["spp"],
+                                accel=orc.make_accel(abi.ACCEL_NONE), max_depth=C1["depth"],
+                                arg_order_rtl=True, portable_trig=True, rr_depth=3)
+    g, o = _f(g_col), _f(o_col)
+    parity_report("config1_rr_depth3", rel_rmse_portable=_rel_rmse(g, o), identical_portable=_identical(g, o),
+                  seeds_equal=float((g_sd == o_sd).mean()),
+                  seeds_changed_vs_plain=float((g_sd != c["portable"][1]).mean()))
+    assert _rel_rmse(g, o) < RMSE_TOL
+    assert _identical(g, o) > 0.999
+    assert (g_sd == o_sd).mean() > 0.999
+    # the roulette draws randoms: the seed streams move on past the plain ones
+    assert (g_sd != c["portable"][1]).mean() > 0.5
+
+
+def test_russian_roulette_rejected_with_wavefront(built_lib):
+    import ptgpu_pc_gb300 as pt
+    with pytest.raises(pt.PtgpuError):
+        pt.Context(16, 16, flags=abi.FLAG_WAVEFRONT, rr_depth=3)

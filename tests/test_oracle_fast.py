@@ -104,3 +104,30 @@ def test_fast_render_equals_plain_render(accel, orc):
         out.append((col, pix, sd))
     assert out[0][0].tobytes() == out[1][0].tobytes()
     assert np.array_equal(out[0][2], out[1][2])
+
+
+def test_oracle_russian_roulette_keeps_the_mean(orc):
+    """The opt-in throughput roulette (rr_depth > 0) is unbiased: over 8 seed
+    replicas the frame mean with rr_depth = 2 agrees with the plain
+    estimator's within 3 combined standard errors, and rr_depth = 0 is the
+    plain estimator bit for bit."""
+    shapes, lc, cam = scenes.icosphere_scene(level=2)
+    w = h = 24
+    c = np.array(cam, abi.CAMERA)
+    c["width"], c["height"] = w, h
+    c = orc.update_camera(c)
+    _, btn, btl, _ = orc.build_bvh(shapes)
+    acc = orc.make_accel(abi.ACCEL_BVH, btn, btl, fast=True)
+    means = {0: [], 2: []}
+    for r in range(8):
+        seeds = orc.make_seeds(60 + r, 2 * w * h)
+        for rr in (0, 2):
+            col, _, _ = orc.render(shapes, lc, c, w, h, seeds, 8, accel=acc, max_depth=8, rr_depth=rr)
+            means[rr].append(col.view(np.float32).mean())
+    a, b = np.array(means[0]), np.array(means[2])
+    se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+    assert abs(a.mean() - b.mean()) <= 3 * se
+    seeds = orc.make_seeds(70, 2 * w * h)
+    p0 = orc.render(shapes, lc, c, w, h, seeds, 2, accel=acc, max_depth=8)
+    p1 = orc.render(shapes, lc, c, w, h, seeds, 2, accel=acc, max_depth=8, rr_depth=0)
+    assert p0[0].tobytes() == p1[0].tobytes()
