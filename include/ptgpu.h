@@ -40,6 +40,7 @@ extern "C" {
 #define PTGPU_E_IO        -5  /* scene file missing or malformed                */
 #define PTGPU_E_RANGE     -6  /* result does not fit the reference layout       */
 #define PTGPU_E_STATE     -7  /* call out of order (e.g. draw before build)     */
+#define PTGPU_E_CANCELED  -8  /* a served request was cancelled                 */
 
 /* ---- reference constants (include/geom.h:29-35, clheader.h:9-15) --------- */
 #define PTGPU_EPSILON      0.01f
@@ -346,6 +347,9 @@ typedef struct {
     int64_t requests_done, builds, evictions, steps;
     int32_t resident_scenes, active_requests, pending_requests, quantum;
     double samples_done;
+    /* slots held now: shape slots of resident scenes, pixel slots of admitted
+     * requests, light records of resident scenes */
+    int64_t shape_slots_used, pixel_slots_used, light_slots_used;
 } ptgpu_server_info;
 
 int  ptgpu_server_create(int32_t device, int64_t budget_bytes, int32_t quantum, uint32_t flags,
@@ -370,6 +374,34 @@ int  ptgpu_server_submit(ptgpu_server *s, const ptgpu_request *r, int64_t *ticke
 int  ptgpu_server_wait(ptgpu_server *s, int64_t ticket, uint32_t *pixels, ptgpu_vec *colors,
                        ptgpu_request_stats *stats);
 int  ptgpu_server_info_get(ptgpu_server *s, ptgpu_server_info *info);
+/* No counterpart in the reference (it has no requests).  Cancels a request
+ * that has not been waited for: a pending one leaves the queue, an active one
+ * ends at the next step boundary, releasing its pixel slots and its hold on
+ * its scene; ptgpu_server_wait then returns PTGPU_E_CANCELED.  A request that
+ * already finished keeps its result.  Callable from any thread. */
+int  ptgpu_server_cancel(ptgpu_server *s, int64_t ticket);
+/* No counterpart in the reference.  Progressive preview: copies the
+ * request's W*H pixels and colours (either may be NULL) as they stand after
+ * its last finished render step, and the passes they hold; a finished request
+ * gives its final image.  PTGPU_E_STATE: not admitted yet (no pass rendered).
+ * Does not end or reserve the ticket.  Callable from any thread. */
+int  ptgpu_server_preview(ptgpu_server *s, int64_t ticket, uint32_t *pixels, ptgpu_vec *colors,
+                          int32_t *passes_done);
+
+/* ---- image output ------------------------------------------------------------ */
+/* The frame as an image file, encoded on the device and copied out once.
+ * PTGPU_IMAGE_PPM: the reference's dump of the display buffer
+ * (smallptGPU.cpp:1238-1257): "P3\n<w> <h>\n255\n", then "<r> <g> <b> " for
+ * every pixel, rows from the top of the image down, no line breaks.
+ * PTGPU_IMAGE_PFM (no counterpart in the reference): the float running mean,
+ * "PF\n<w> <h>\n-1.0\n" and RGB float32 little-endian, bottom row first.
+ * E_STATE before the first drawn frame. */
+#define PTGPU_IMAGE_PPM 0
+#define PTGPU_IMAGE_PFM 1
+/* into a caller buffer: *size is its capacity in bytes; buf NULL (or too
+ * small: E_INVAL) answers the size in *size */
+int  ptgpu_encode_image(ptgpu_ctx *ctx, int32_t format, void *buf, uint64_t *size);
+int  ptgpu_write_image(ptgpu_ctx *ctx, const char *path, int32_t format);
 
 /* ---- BVH build without device allocation ----------------------------------- */
 /* No counterpart in the reference.  The LBVH build of ptgpu_build(ctx,
@@ -425,7 +457,7 @@ PTGPU_SA(sizeof(ptgpu_batch_info) == 40, "ptgpu_batch_info is 40 bytes");
 PTGPU_SA(sizeof(ptgpu_request) == 112, "ptgpu_request is 112 bytes");
 PTGPU_SA(offsetof(ptgpu_request, camera) == 32, "ptgpu_request.camera at 32");
 PTGPU_SA(sizeof(ptgpu_request_stats) == 24, "ptgpu_request_stats is 24 bytes");
-PTGPU_SA(sizeof(ptgpu_server_info) == 72, "ptgpu_server_info is 72 bytes");
+PTGPU_SA(sizeof(ptgpu_server_info) == 96, "ptgpu_server_info is 96 bytes");
 #undef PTGPU_SA
 
 #endif /* PTGPU_H */

@@ -31,7 +31,8 @@ EXPORTS = [
     "ptgpu_batch_get_colors", "ptgpu_batch_get_bvh", "ptgpu_batch_info_get",
     "ptgpu_server_create", "ptgpu_server_destroy", "ptgpu_server_add_scene", "ptgpu_server_add_scene_file",
     "ptgpu_server_submit",
-    "ptgpu_server_wait", "ptgpu_server_info_get",
+    "ptgpu_server_wait", "ptgpu_server_info_get", "ptgpu_server_cancel", "ptgpu_server_preview",
+    "ptgpu_encode_image", "ptgpu_write_image",
 ]
 
 _lib = None
@@ -45,7 +46,7 @@ class PtgpuError(RuntimeError):
 
 def _status_name(s):
     return {0: "ok", -1: "E_INVAL", -2: "E_OOM", -3: "E_DEVICE", -4: "E_TIMEOUT",
-            -5: "E_IO", -6: "E_RANGE", -7: "E_STATE"}.get(s, "E_?")
+            -5: "E_IO", -6: "E_RANGE", -7: "E_STATE", -8: "E_CANCELED"}.get(s, "E_?")
 
 
 def lib():
@@ -90,12 +91,16 @@ def lib():
         L.ptgpu_server_submit.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_int64)]
         L.ptgpu_server_wait.argtypes = [vp, ctypes.c_int64, vp, vp, vp]
         L.ptgpu_server_info_get.argtypes = [vp, vp]
+        L.ptgpu_server_cancel.argtypes = [vp, ctypes.c_int64]
+        L.ptgpu_server_preview.argtypes = [vp, ctypes.c_int64, vp, vp, ctypes.POINTER(i32)]
         L.ptgpu_get_bvh.argtypes = [vp, vp, vp]
         L.ptgpu_set_bvh.argtypes = [vp, vp, vp, u32]
         L.ptgpu_get_kdtree.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]
         L.ptgpu_get_kdtree_wide.argtypes = [vp, vp, ctypes.POINTER(i32), vp, ctypes.POINTER(i32)]
         L.ptgpu_last_build_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
         L.ptgpu_set_wait_limit.argtypes = [vp, u32]
+        L.ptgpu_encode_image.argtypes = [vp, i32, vp, ctypes.POINTER(ctypes.c_uint64)]
+        L.ptgpu_write_image.argtypes = [vp, ctypes.c_char_p, i32]
         L.ptgpu_make_seeds.argtypes = [ctypes.c_uint64, vp, u32]
         L.ptgpu_set_seeds.argtypes = [vp, vp]
         L.ptgpu_get_seeds.argtypes = [vp, vp]
@@ -217,6 +222,18 @@ class Context:
 
     def build(self, accel=abi.ACCEL_BVH, flags=0):
         _check(lib().ptgpu_build(self._h, accel, flags))
+
+    def encode_image(self, fmt=0):
+        """The frame as image file bytes (abi.IMAGE_PPM: the reference's P3
+        dump; abi.IMAGE_PFM: the float running mean)."""
+        n = ctypes.c_uint64()
+        _check(lib().ptgpu_encode_image(self._h, fmt, None, ctypes.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        _check(lib().ptgpu_encode_image(self._h, fmt, _p(buf), ctypes.byref(n)))
+        return buf.tobytes()
+
+    def write_image(self, path, fmt=0):
+        _check(lib().ptgpu_write_image(self._h, str(path).encode(), fmt))
 
     def set_wait_limit(self, polls):
         """Look-back polls before a build gives up with E_TIMEOUT (0: at the
@@ -461,6 +478,22 @@ class Server:
         _check(lib().ptgpu_server_wait(self._h, ticket, px.ctypes.data if px is not None else None,
                                        col.ctypes.data if col is not None else None, st.ctypes.data))
         return px, col, {k: st[k][0].item() for k in abi.REQUEST_STATS.names}
+
+    def cancel(self, ticket):
+        """Cancels a request; its wait() then raises E_CANCELED."""
+        _check(lib().ptgpu_server_cancel(self._h, ctypes.c_int64(ticket)))
+
+    def preview(self, ticket, want_pixels=True, want_colors=True):
+        """The request's image after its last finished step: (pixels,
+        colours, passes)."""
+        w, h = self._sizes[ticket]
+        px = np.zeros(w * h, np.uint32) if want_pixels else None
+        col = np.zeros((w * h, 3), np.float32) if want_colors else None
+        n = ctypes.c_int32()
+        _check(lib().ptgpu_server_preview(self._h, ctypes.c_int64(ticket),
+                                          px.ctypes.data if px is not None else None,
+                                          col.ctypes.data if col is not None else None, ctypes.byref(n)))
+        return px, col, n.value
 
     def info(self):
         out = np.zeros(1, abi.SERVER_INFO)

@@ -11,6 +11,7 @@ SPHERE, TRIANGLE = 0, 1
 DIFF, SPEC, REFR = 0, 1, 2
 ACCEL_NONE, ACCEL_BVH, ACCEL_KDTREE = 0, 1, 2
 WAIT_LIMIT_DEFAULT = 4194304      # PTGPU_WAIT_LIMIT_DEFAULT
+IMAGE_PPM, IMAGE_PFM = 0, 1       # PTGPU_IMAGE_*
 
 VEC = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4")])
 RAY = np.dtype({"names": ["o", "d"], "formats": [("<f4", 3), ("<f4", 3)],
@@ -98,14 +99,16 @@ REQUEST_STATS = np.dtype({
 
 SERVER_INFO = np.dtype({
     "names": ["budget_bytes", "bytes_in_use", "requests_done", "builds", "evictions", "steps",
-              "resident_scenes", "active_requests", "pending_requests", "quantum", "samples_done"],
-    "formats": ["<i8"] * 6 + ["<i4"] * 4 + ["<f8"],
-    "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 60, 64],
-    "itemsize": 72,
+              "resident_scenes", "active_requests", "pending_requests", "quantum", "samples_done",
+              "shape_slots_used", "pixel_slots_used", "light_slots_used"],
+    "formats": ["<i8"] * 6 + ["<i4"] * 4 + ["<f8"] + ["<i8"] * 3,
+    "offsets": [0, 8, 16, 24, 32, 40, 48, 52, 56, 60, 64, 72, 80, 88],
+    "itemsize": 96,
 })
 
 # status codes (include/ptgpu.h)
 OK, E_INVAL, E_OOM, E_DEVICE, E_TIMEOUT, E_IO, E_RANGE, E_STATE = 0, -1, -2, -3, -4, -5, -6, -7
+E_CANCELED = -8
 
 FLAG_WAVEFRONT = 0x1
 FLAG_MORTON_DELTA = 0x2        # reserved: ptgpu_build answers E_INVAL

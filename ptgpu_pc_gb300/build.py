@@ -12,7 +12,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libptgpu.so")
 
-CU_SOURCES = ["lbvh.cu", "trace.cu", "wavefront.cu", "noalloc.cu", "batch.cu", "kd_gpu.cu", "ingest.cu"]
+CU_SOURCES = ["lbvh.cu", "trace.cu", "wavefront.cu", "noalloc.cu", "batch.cu", "kd_gpu.cu", "ingest.cu",
+              "image.cu"]
 CPP_SOURCES = ["api.cpp", "kdtree.cpp", "loader.cpp", "batch.cpp", "server.cpp"]
 HEADERS = ["device.cuh", "types.h", "lbvh.h", "lbvh_topo.cuh", "host.h", "devbuf.h", "ingest.h",
            "range_alloc.h"]

@@ -116,6 +116,7 @@ struct ptgpu_ctx {
     int w = 0, h = 0;
     DevBuf d_colors, d_pixels, d_seeds, d_err, d_pixctr, d_wf;
     DevBuf d_cost, d_order, d_order_scr;   // per-pixel work, next hand-out order
+    DevBuf d_img, d_rowoff;                 // an encoded image, its PPM row offsets
     bool order_valid = false;
     uint32_t *h_pixels = nullptr;
     int current_sample = 0;
@@ -167,6 +168,7 @@ const char *ptgpu_status_string(int s) {
     case PTGPU_E_IO: return "scene i/o error";
     case PTGPU_E_RANGE: return "result does not fit the reference layout";
     case PTGPU_E_STATE: return "call out of order";
+    case PTGPU_E_CANCELED: return "request cancelled";
     default: return "unknown status";
     }
 }
@@ -655,6 +657,61 @@ int ptgpu_get_kdtree_wide(ptgpu_ctx *c, ptgpu_kd_node_wide *nodes, int32_t *node
     *node_cnt = cnt;
     *kn_cnt = kcnt;
     return PTGPU_OK;
+}
+
+int ptgpu_encode_image(ptgpu_ctx *c, int32_t format, void *buf, uint64_t *size) {
+    if (!c || !size) return fail(PTGPU_E_INVAL, "null argument");
+    if (format != PTGPU_IMAGE_PPM && format != PTGPU_IMAGE_PFM) return fail(PTGPU_E_INVAL, "unknown image format");
+    if (c->current_sample <= 0) return fail(PTGPU_E_STATE, "no frame has been drawn");
+    cudaSetDevice(c->device);
+    char header[80];
+    int hl;
+    uint64_t body;
+    if (format == PTGPU_IMAGE_PPM) {
+        hl = std::snprintf(header, sizeof(header), "P3\n%d %d\n%d\n", c->w, c->h, 255);
+        CK(c->d_rowoff.ensure(((size_t)c->h + 1) * sizeof(uint64_t)));
+        CK(launch_ppm_length(c->d_pixels.as<uint32_t>(), c->w, c->h, c->d_rowoff.as<uint64_t>(), c->stream));
+        CK(cudaMemcpyAsync(&body, c->d_rowoff.as<uint64_t>() + c->h, sizeof(body), cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    } else {
+        hl = std::snprintf(header, sizeof(header), "PF\n%d %d\n-1.0\n", c->w, c->h);
+        body = (uint64_t)c->w * c->h * 3 * sizeof(float);
+    }
+    const uint64_t need = (uint64_t)hl + body;
+    if (!buf) { *size = need; return PTGPU_OK; }
+    if (*size < need) { *size = need; return fail(PTGPU_E_INVAL, "image buffer too small"); }
+    std::memcpy(buf, header, (size_t)hl);
+    CK(c->d_img.ensure(body ? body : 1));
+    if (format == PTGPU_IMAGE_PPM)
+        CK(launch_ppm_write(c->d_pixels.as<uint32_t>(), c->w, c->h, c->d_rowoff.as<uint64_t>(), c->d_img.as<char>(),
+                            c->stream));
+    else
+        CK(launch_pfm(c->d_colors.as<ptgpu_vec>(), c->w, c->h, c->d_img.as<float>(), c->sm_count, c->stream));
+    CK(cudaMemcpyAsync(static_cast<char *>(buf) + hl, c->d_img.p, body, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *size = need;
+    return PTGPU_OK;
+}
+
+int ptgpu_write_image(ptgpu_ctx *c, const char *path, int32_t format) {
+    if (!c || !path) return fail(PTGPU_E_INVAL, "null argument");
+    uint64_t size = 0;
+    int st = ptgpu_encode_image(c, format, nullptr, &size);
+    if (st) return st;
+    std::vector<char> bytes;
+    try {
+        bytes.resize(size);
+    } catch (const std::bad_alloc &) {
+        return fail(PTGPU_E_OOM, "out of host memory for the image");
+    }
+    st = ptgpu_encode_image(c, format, bytes.data(), &size);
+    if (st) return st;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(PTGPU_E_IO, std::string("cannot open image file: ") + path);
+    const size_t wrote = std::fwrite(bytes.data(), 1, bytes.size(), f);
+    const bool ok = std::fclose(f) == 0 && wrote == bytes.size();
+    return ok ? PTGPU_OK : fail(PTGPU_E_IO, std::string("cannot write image file: ") + path);
 }
 
 int ptgpu_set_seeds(ptgpu_ctx *c, const uint32_t *seeds) {

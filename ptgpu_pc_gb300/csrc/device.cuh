@@ -191,9 +191,16 @@ struct ShortStack {
     __device__ __forceinline__ int get(int i) const { return i < SHORT ? sh[i * LANES] : loc[i - SHORT]; }
 };
 
-// entries of a lane's stack kept in shared memory (0: all in local memory)
+// entries of a lane's stack kept in shared memory (0: all in local memory):
+// the closest-hit kernel (2^24 random rays against 4M triangles: 20.68 ->
+// 18.74 ms with 16) and the lane tracer (0: 8 / 16 / 24 entries measured
+// 29.2 / 29.3 / 29.4 against 28.8 ms per benchmark frame -- the shared
+// memory they take comes out of the L1 that caches the scene's nodes)
 #ifndef PTGPU_SHORT_STACK
 #define PTGPU_SHORT_STACK 16
+#endif
+#ifndef PTGPU_RENDER_SHORT_STACK
+#define PTGPU_RENDER_SHORT_STACK 0
 #endif
 
 // A query in flight: the ray, the best hit so far and the traversal

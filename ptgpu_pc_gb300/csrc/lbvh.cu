@@ -755,15 +755,28 @@ __device__ __forceinline__ uint32_t lookback_digit(uint32_t *status, int tile, i
     return excl;
 }
 
+// Ranking chains per warp: a warp's items are ranked as kSortChains
+// independent runs (the first and the second half of its items), each with
+// its own per-digit counts, interleaved item by item, so that one run's
+// shared-memory round trips (lane mask, count load, count store) overlap the
+// other's; the second run's ranks are then offset by the first run's counts.
+#ifndef PTGPU_SORT_CHAINS
+#define PTGPU_SORT_CHAINS 2
+#endif
+constexpr int kSortChains = PTGPU_SORT_CHAINS;
+static_assert(kSortChains == 1 || kSortChains == 2, "one or two ranking chains");
+constexpr int kChainItems = (kSortItems + kSortChains - 1) / kSortChains;
+
 struct SortSmem {
-    uint32_t warp_hist[kSortWarps][256];
+    uint32_t warp_hist[kSortWarps][256];          // the first chain's counts, then the warp's
+    uint32_t chain_hist[kSortWarps][kSortChains > 1 ? 256 : 4];   // the second chain's counts
     uint32_t digit_start[256];
     uint32_t tile_excl[256];
     uint32_t scan_tmp[32];
     union {
-        // ranking: per-warp lane masks of each digit, two sets used by
-        // alternate items so that clearing one never races with filling it
-        uint32_t match[2][kSortWarps][256];
+        // ranking: per-warp lane masks of each digit and chain, two sets used
+        // by alternate items so that clearing one never races with filling it
+        uint32_t match[2][kSortChains][kSortWarps][256];
         // scatter: the tile in sorted order
         struct {
             uint32_t keys[kSortTile];
@@ -799,7 +812,11 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     static_assert(kSortWarps * 256 % (4 * kSortThreads) == 0, "16-byte clears");
     const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
     for (int i = tid; i < kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.warp_hist[0][0])[i] = zero4;
-    for (int i = tid; i < 2 * kSortWarps * 64; i += kSortThreads) reinterpret_cast<uint4 *>(&sm.u.match[0][0][0])[i] = zero4;
+    if (kSortChains > 1)
+        for (int i = tid; i < kSortWarps * 64; i += kSortThreads)
+            reinterpret_cast<uint4 *>(&sm.chain_hist[0][0])[i] = zero4;
+    for (int i = tid; i < 2 * kSortChains * kSortWarps * 64; i += kSortThreads)
+        reinterpret_cast<uint4 *>(&sm.u.match[0][0][0][0])[i] = zero4;
     // global digit offsets for this pass
     const bool dig_thread = kSortThreads == 256 || tid < 256;
     uint32_t gcount = dig_thread ? st->hist[pass][tid] : 0u;
@@ -837,27 +854,62 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     goff = block_excl_scan256(gcount, sm.scan_tmp);
 #endif
 #pragma unroll
-    for (int j = 0; j < kSortItems; ++j) {
-        const int idx = base + w * 32 * kSortItems + j * 32 + lane;
-        const bool valid = idx < n;
-        uint32_t dig = (key[j] >> shift) & 255u;
-        // lanes with the same digit: each sets its bit in the digit's mask
-        uint32_t *mask = &sm.u.match[j & 1][w][dig];
-        if (valid) atomicOr(mask, 1u << lane);
-        __syncwarp();
-        rank[j] = 0xffffffffu;
-        uint32_t prev = 0u;
-        unsigned peers = 0u;
-        if (valid) {
-            peers = *mask;
-            prev = sm.warp_hist[w][dig];
-            rank[j] = prev + (uint32_t)__popc(peers & lt_mask);
+    for (int k = 0; k < kChainItems; ++k) {
+        // item k of every chain: lanes with the same digit each set their bit
+        // in the digit's mask
+        uint32_t *mask[kSortChains];
+        uint32_t dig[kSortChains];
+        bool valid[kSortChains];
+#pragma unroll
+        for (int c = 0; c < kSortChains; ++c) {
+            const int j = c * kChainItems + k;
+            valid[c] = false;
+            if (j < kSortItems) {
+                const int64_t idx = base + (int64_t)w * 32 * kSortItems + j * 32 + lane;
+                valid[c] = idx < n;
+                dig[c] = (key[j] >> shift) & 255u;
+                mask[c] = &sm.u.match[k & 1][c][w][dig[c]];
+                if (valid[c]) atomicOr(mask[c], 1u << lane);
+            }
         }
         __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) {
-            sm.warp_hist[w][dig] = prev + (uint32_t)__popc(peers);
-            *mask = 0u;
+        uint32_t prev[kSortChains];
+        unsigned peers[kSortChains];
+#pragma unroll
+        for (int c = 0; c < kSortChains; ++c) {
+            const int j = c * kChainItems + k;
+            if (j >= kSortItems) continue;
+            rank[j] = 0xffffffffu;
+            prev[c] = 0u;
+            peers[c] = 0u;
+            if (valid[c]) {
+                uint32_t *hist = c == 0 ? &sm.warp_hist[w][0] : &sm.chain_hist[w][0];
+                peers[c] = *mask[c];
+                prev[c] = hist[dig[c]];
+                rank[j] = prev[c] + (uint32_t)__popc(peers[c] & lt_mask);
+            }
         }
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < kSortChains; ++c) {
+            const int j = c * kChainItems + k;
+            if (j < kSortItems && valid[c] && lane == __ffs(peers[c]) - 1) {
+                uint32_t *hist = c == 0 ? &sm.warp_hist[w][0] : &sm.chain_hist[w][0];
+                hist[dig[c]] = prev[c] + (uint32_t)__popc(peers[c]);
+                *mask[c] = 0u;
+            }
+        }
+    }
+    if (kSortChains > 1) {
+        // the second chain's items follow the first chain's in the warp's
+        // order: offset their ranks by the first chain's counts, then make
+        // warp_hist the warp's totals
+        __syncwarp();
+#pragma unroll
+        for (int j = kChainItems; j < kSortItems; ++j)
+            if (rank[j] != 0xffffffffu) rank[j] += sm.warp_hist[w][(key[j] >> shift) & 255u];
+        __syncwarp();
+        for (int d = lane; d < 256; d += 32) sm.warp_hist[w][d] += sm.chain_hist[w][d];
     }
     __syncthreads();
     // per-digit counts: exclusive prefix over warps, tile total

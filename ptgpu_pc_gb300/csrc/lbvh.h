@@ -143,6 +143,14 @@ struct RenderArgs {
     int32_t n_scenes;
 };
 cudaError_t launch_render(const RenderArgs &a, int block, cudaStream_t s);
+// Image encoding (image.cu).  PPM "P3" text of the RGBA8 pixels: row_off
+// (h + 1 words) gets each output row's character offset and the total in
+// row_off[h]; the text (without the header) is then written to out.
+cudaError_t launch_ppm_length(const uint32_t *pixels, int w, int h, uint64_t *row_off, cudaStream_t s);
+cudaError_t launch_ppm_write(const uint32_t *pixels, int w, int h, const uint64_t *row_off, char *out,
+                             cudaStream_t s);
+// PFM float RGB of the row-flipped colour buffer, bottom row first (3*w*h floats)
+cudaError_t launch_pfm(const ptgpu_vec *colors, int w, int h, float *out, int sm_count, cudaStream_t s);
 // The next frame's hand-out order from this frame's per-pixel work: pixels in
 // decreasing work (logarithmic classes, 8 per power of two; any order inside
 // a class), so the longest pixel chains start first and the frame ends on

@@ -43,6 +43,13 @@ struct RangeAlloc {
             }
         }
     }
+    // length of the free range that ends at the capacity (0 if the last
+    // element is in use): growing by g makes a free range of free_tail() + g
+    int64_t free_tail() const {
+        if (free_.empty()) return 0;
+        auto last = std::prev(free_.end());
+        return last->first + last->second == capacity ? last->second : 0;
+    }
     void grow(int64_t new_cap) {   // the new tail becomes free
         if (new_cap <= capacity) return;
         used += new_cap - capacity;   // release() below takes it off again

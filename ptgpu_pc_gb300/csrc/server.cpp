@@ -106,8 +106,20 @@ struct Request {
     int built = 0;
     int status = PTGPU_OK;
     bool finished = false;
+    std::atomic<bool> cancel{false};     // set by ptgpu_server_cancel, acted on by the worker
     std::vector<uint32_t> pixels;
     std::vector<ptgpu_vec> colors;
+};
+
+// A progressive-preview copy of a request's image, made by the worker
+// between two steps (ptgpu_server_preview waits for it).
+struct PreviewJob {
+    std::shared_ptr<Request> q;
+    uint32_t *pixels = nullptr;
+    ptgpu_vec *colors = nullptr;
+    int passes = 0;
+    int status = PTGPU_OK;
+    bool done = false;
 };
 
 int cuda_fail(cudaError_t e, const char *what) {
@@ -130,6 +142,7 @@ struct ptgpu_server {
     bool stop = false;
     int64_t next_ticket = 1;
     std::deque<std::shared_ptr<Request>> pending;                 // arrival order
+    std::deque<std::shared_ptr<PreviewJob>> previews;             // to serve between steps
     std::unordered_map<int64_t, std::shared_ptr<Request>> tickets;
     std::vector<std::unique_ptr<SceneEntry>> scenes;              // by id (the vector: mu)
     // worker-only state
@@ -147,6 +160,8 @@ struct ptgpu_server {
     int64_t done_count = 0, builds = 0, evictions = 0, steps = 0;
     double samples_done = 0.0;
     int last_error = PTGPU_OK;
+    // the worker's slot counts as of its last release or admission (mu)
+    int64_t shape_slots_used = 0, pixel_slots_used = 0, light_slots_used = 0;
 
     int64_t bytes_in_use() const {
         return shape_slots.capacity * kSlotBytes + pix_slots.capacity * kPixBytes +
@@ -161,14 +176,16 @@ SceneEntry &scene_of(ptgpu_server *s, int id) {
     return *s->scenes[id];
 }
 
-// Grows the shape arenas to hold `need` more slots, within the budget.
+// Grows the shape arenas so that `need` contiguous slots fit (the free
+// range at the end of the arena counts), within the budget.
 int grow_shapes(ptgpu_server *s, int64_t need) {
     const int64_t cap = s->shape_slots.capacity;
-    int64_t want = std::max<int64_t>(cap * 2, cap + need);
+    const int64_t min_cap = cap + need - s->shape_slots.free_tail();
+    int64_t want = std::max<int64_t>(cap * 2, min_cap);
     want = std::max<int64_t>(want, 4096);
     const int64_t room = (s->budget - s->bytes_in_use()) / kSlotBytes + cap;
     if (want > room) want = room;
-    if (want < cap + need) return PTGPU_E_OOM;
+    if (want < min_cap) return PTGPU_E_OOM;
     Arena *as[] = {&s->nodes, &s->prims, &s->prim_id, &s->mats, &s->prims0};
     for (Arena *a : as) {
         cudaError_t e = a->grow(cap, want, s->stream);
@@ -180,11 +197,12 @@ int grow_shapes(ptgpu_server *s, int64_t need) {
 
 int grow_pixels(ptgpu_server *s, int64_t need) {
     const int64_t cap = s->pix_slots.capacity;
-    int64_t want = std::max<int64_t>(cap * 2, cap + need);
+    const int64_t min_cap = cap + need - s->pix_slots.free_tail();
+    int64_t want = std::max<int64_t>(cap * 2, min_cap);
     want = std::max<int64_t>(want, 16384);
     const int64_t room = (s->budget - s->bytes_in_use()) / kPixBytes + cap;
     if (want > room) want = room;
-    if (want < cap + need) return PTGPU_E_OOM;
+    if (want < min_cap) return PTGPU_E_OOM;
     Arena *as[] = {&s->colors, &s->pixels, &s->seeds};
     for (Arena *a : as) {
         cudaError_t e = a->grow(cap, want, s->stream);
@@ -196,10 +214,11 @@ int grow_pixels(ptgpu_server *s, int64_t need) {
 
 int grow_lights(ptgpu_server *s, int64_t need) {
     const int64_t cap = s->light_slots.capacity;
-    int64_t want = std::max<int64_t>(std::max<int64_t>(cap * 2, cap + need), 256);
+    const int64_t min_cap = cap + need - s->light_slots.free_tail();
+    int64_t want = std::max<int64_t>(std::max<int64_t>(cap * 2, min_cap), 256);
     const int64_t room = (s->budget - s->bytes_in_use()) / (int64_t)sizeof(LightRec) + cap;
     if (want > room) want = room;
-    if (want < cap + need) return PTGPU_E_OOM;
+    if (want < min_cap) return PTGPU_E_OOM;
     cudaError_t e = s->lights.grow(cap, want, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "light arena");
     s->light_slots.grow(want);
@@ -365,8 +384,16 @@ int build_scene(ptgpu_server *s, int id) {
     return PTGPU_OK;
 }
 
+// (worker thread, mu held) the slot counts that ptgpu_server_info_get reports
+void publish_usage_locked(ptgpu_server *s) {
+    s->shape_slots_used = s->shape_slots.used;
+    s->pixel_slots_used = s->pix_slots.used;
+    s->light_slots_used = s->light_slots.used;
+}
+
 void finish(ptgpu_server *s, const std::shared_ptr<Request> &r, int status) {
     std::lock_guard<std::mutex> lk(s->mu);
+    publish_usage_locked(s);
     r->status = status;
     r->finished = true;
     r->t_done = Clock::now();
@@ -377,12 +404,86 @@ void finish(ptgpu_server *s, const std::shared_ptr<Request> &r, int status) {
     s->cv_done.notify_all();
 }
 
+// Cancelled requests that have not been admitted leave the queue (only the
+// worker removes requests from it, so no admission is in flight here).
+void drop_cancelled_pending(ptgpu_server *s) {
+    std::vector<std::shared_ptr<Request>> gone;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto it = s->pending.begin(); it != s->pending.end();) {
+            if ((*it)->cancel) { gone.push_back(*it); it = s->pending.erase(it); }
+            else ++it;
+        }
+    }
+    for (auto &q : gone) finish(s, q, PTGPU_E_CANCELED);
+}
+
+// Active requests that were cancelled give their pixel slots back and end
+// before the next step.
+void drop_cancelled_active(ptgpu_server *s) {
+    std::vector<std::shared_ptr<Request>> keep;
+    for (auto &q : s->active) {
+        if (!q->cancel) { keep.push_back(q); continue; }
+        s->pix_slots.release(q->pix_base, (int64_t)q->r.width * q->r.height);
+        scene_of(s, q->r.scene).users--;
+        finish(s, q, PTGPU_E_CANCELED);
+    }
+    s->active.swap(keep);
+    s->n_active = (int)s->active.size();
+}
+
+// Serves the queued preview copies: an active request's image as of its
+// last finished step, a finished one's final image.
+void serve_previews(ptgpu_server *s) {
+    std::deque<std::shared_ptr<PreviewJob>> jobs;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        jobs.swap(s->previews);
+    }
+    for (auto &j : jobs) {
+        Request &q = *j->q;
+        const int64_t px = (int64_t)q.r.width * q.r.height;
+        bool active = false;
+        for (auto &a : s->active) active = active || a.get() == &q;
+        bool fin;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            fin = q.finished;
+        }
+        if (active) {
+            cudaError_t e = cudaSuccess;
+            if (j->pixels)
+                e = cudaMemcpyAsync(j->pixels, s->pixels.buf.as<uint32_t>() + q.pix_base, px * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess && j->colors)
+                e = cudaMemcpyAsync(j->colors, s->colors.buf.as<ptgpu_vec>() + q.pix_base,
+                                    px * sizeof(ptgpu_vec), cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            j->passes = q.done_passes;
+            j->status = e == cudaSuccess ? PTGPU_OK : cuda_fail(e, "preview copy");
+        } else if (fin && q.status == PTGPU_OK) {
+            if (j->pixels) std::memcpy(j->pixels, q.pixels.data(), px * sizeof(uint32_t));
+            if (j->colors) std::memcpy(j->colors, q.colors.data(), px * sizeof(ptgpu_vec));
+            j->passes = q.r.spp;
+        } else if (fin) {
+            j->status = q.status;
+        } else {
+            j->status = PTGPU_E_STATE;     // not admitted yet: no pass rendered
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        j->done = true;
+        s->cv_done.notify_all();
+    }
+}
+
 // Admits pending requests in arrival order while they fit.
 void admit(ptgpu_server *s) {
+    drop_cancelled_pending(s);
     for (;;) {
         std::shared_ptr<Request> r;
         {
             std::lock_guard<std::mutex> lk(s->mu);
+            publish_usage_locked(s);
             if (s->pending.empty() || s->active.size() >= (size_t)kMaxSegments) return;
             r = s->pending.front();
         }
@@ -443,7 +544,9 @@ void admit(ptgpu_server *s) {
 
 // One step: up to `quantum` passes of every admitted request, one launch.
 int step(ptgpu_server *s) {
+    drop_cancelled_active(s);
     const int S = (int)s->active.size();
+    if (S == 0) return PTGPU_OK;
     std::vector<BatchScene> recs(S);
     std::vector<int64_t> start(S + 1, 0);
     int depth = 0;
@@ -536,9 +639,16 @@ void worker_main(ptgpu_server *s) {
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty() || !s->active.empty(); });
-            if (s->stop && s->pending.empty() && s->active.empty()) return;
+            s->cv_work.wait(lk, [&] {
+                return s->stop || !s->pending.empty() || !s->active.empty() || !s->previews.empty();
+            });
+            if (s->stop && s->pending.empty() && s->active.empty()) {
+                lk.unlock();
+                serve_previews(s);
+                return;
+            }
         }
+        serve_previews(s);
         admit(s);
         if (s->active.empty()) {
             // nothing admissible now: wait for a new submission
@@ -717,9 +827,43 @@ int ptgpu_server_wait(ptgpu_server *s, int64_t ticket, uint32_t *pixels, ptgpu_v
         stats->steps = q->steps;
         stats->built = q->built;
     }
+    if (q->status == PTGPU_E_CANCELED) return record_error(q->status, "request cancelled");
     if (q->status != PTGPU_OK) return record_error(q->status, "request failed");
     if (pixels) std::memcpy(pixels, q->pixels.data(), q->pixels.size() * sizeof(uint32_t));
     if (colors) std::memcpy(colors, q->colors.data(), q->colors.size() * sizeof(ptgpu_vec));
+    return PTGPU_OK;
+}
+
+int ptgpu_server_cancel(ptgpu_server *s, int64_t ticket) {
+    if (!s) return record_error(PTGPU_E_INVAL, "null server");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->tickets.find(ticket);
+        if (it == s->tickets.end()) return record_error(PTGPU_E_INVAL, "unknown ticket");
+        it->second->cancel = true;
+    }
+    s->cv_work.notify_all();
+    return PTGPU_OK;
+}
+
+int ptgpu_server_preview(ptgpu_server *s, int64_t ticket, uint32_t *pixels, ptgpu_vec *colors,
+                         int32_t *passes_done) {
+    if (!s) return record_error(PTGPU_E_INVAL, "null server");
+    auto job = std::make_shared<PreviewJob>();
+    job->pixels = pixels;
+    job->colors = colors;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->tickets.find(ticket);
+        if (it == s->tickets.end()) return record_error(PTGPU_E_INVAL, "unknown ticket");
+        job->q = it->second;
+        s->previews.push_back(job);
+        s->cv_work.notify_all();
+        s->cv_done.wait(lk, [&] { return job->done; });
+    }
+    if (passes_done) *passes_done = job->passes;
+    if (job->status == PTGPU_E_STATE) return record_error(PTGPU_E_STATE, "request not admitted yet");
+    if (job->status != PTGPU_OK) return record_error(job->status, "request failed or preview copy failed");
     return PTGPU_OK;
 }
 
@@ -740,6 +884,9 @@ int ptgpu_server_info_get(ptgpu_server *s, ptgpu_server_info *info) {
     info->pending_requests = (int32_t)s->pending.size();
     info->quantum = s->quantum;
     info->samples_done = s->samples_done;
+    info->shape_slots_used = s->shape_slots_used;
+    info->pixel_slots_used = s->pixel_slots_used;
+    info->light_slots_used = s->light_slots_used;
     return PTGPU_OK;
 }
 

@@ -122,11 +122,11 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
     q.any = 0; q.hit = 0; q.skip = -1;
-#if PTGPU_SHORT_STACK > 0
+#if PTGPU_RENDER_SHORT_STACK > 0
     // the bottom of each lane's traversal stack in shared memory, the rest in
     // local memory (ShortStack)
-    __shared__ int s_stack[PTGPU_SHORT_STACK][128];
-    ShortStack<STACK, PTGPU_SHORT_STACK, 128> stack;
+    __shared__ int s_stack[PTGPU_RENDER_SHORT_STACK][128];
+    ShortStack<STACK, PTGPU_RENDER_SHORT_STACK, 128> stack;
     stack.sh = &s_stack[0][threadIdx.x];
 #else
     LocalStack<STACK> stack;

@@ -145,6 +145,7 @@ int shim_ra_alloc(void *a, int64_t n, int64_t *start) {
 }
 void shim_ra_release(void *a, int64_t start, int64_t n) { static_cast<ptgpu::RangeAlloc *>(a)->release(start, n); }
 int64_t shim_ra_used(void *a) { return static_cast<ptgpu::RangeAlloc *>(a)->used; }
+int64_t shim_ra_free_tail(void *a) { return static_cast<ptgpu::RangeAlloc *>(a)->free_tail(); }
 // the free ranges in address order as (start, length) pairs; returns their count
 int shim_ra_free(void *a, int64_t *out, int max_pairs) {
     int k = 0;

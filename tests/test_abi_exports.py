@@ -45,7 +45,7 @@ def test_abi_version_without_a_device(built_lib):
                                        ("KD_NODE", 36), ("KD_NODE_WIDE", 48), ("CONFIG", 40),
                                        ("SCENE", 120),
                                        ("BATCH_INFO", 40), ("REQUEST", 112), ("REQUEST_STATS", 24),
-                                       ("SERVER_INFO", 72)])
+                                       ("SERVER_INFO", 96)])
 def test_binding_struct_sizes(name, size):
     from ptgpu_pc_gb300 import abi
     assert getattr(abi, name).itemsize == size

@@ -42,6 +42,8 @@ def shim(tmp_path_factory):
     L.shim_ra_used.argtypes = [vp]
     L.shim_ra_used.restype = ctypes.c_int64
     L.shim_ra_free.argtypes = [vp, vp, ctypes.c_int]
+    L.shim_ra_free_tail.argtypes = [vp]
+    L.shim_ra_free_tail.restype = ctypes.c_int64
     L.shim_obj_get.argtypes = [vp, vp]
     L.shim_read_scene_compact.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp]
     L.shim_compact_get.argtypes = [vp]
@@ -343,7 +345,11 @@ def test_server_slot_allocator_first_fit(shim):
                 busy[s:s + n] = False
             assert shim.shim_ra_used(a) == int(busy.sum())
             k = shim.shim_ra_free(a, out.ctypes.data, 4096)
-            assert [tuple(x) for x in out[:2 * k].reshape(-1, 2)] == _free_runs(busy)
+            runs = _free_runs(busy)
+            assert [tuple(x) for x in out[:2 * k].reshape(-1, 2)] == runs
+            # the free run that reaches the capacity (what growth extends)
+            tail = runs[-1][1] if runs and runs[-1][0] + runs[-1][1] == len(busy) else 0
+            assert shim.shim_ra_free_tail(a) == tail
         # releasing everything leaves one range over the whole capacity
         for s, n in live:
             shim.shim_ra_release(a, s, n)
