@@ -289,6 +289,25 @@ def run_reference(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def bench_lbvh(pt, abi, scenes, torch, warmup, steps, n=None):
+    """LBVH builds of n seeded random triangles (config 3's soup): device time
+    of each build (CUDA events in the library), mean over `steps` after
+    `warmup` builds."""
+    n = n or LBVH_N
+    shapes = scenes.triangle_soup(n, seed=3)
+    ctx = pt.Context(8, 8)
+    ctx.set_shapes(shapes, 0)
+    del shapes
+    times = []
+    for i in range(warmup + steps):
+        ctx.build(abi.ACCEL_BVH)
+        if i >= warmup:
+            times.append(ctx.last_build_ms())
+    ms = float(np.mean(times))
+    return ctx, {"metric": "LBVH Mtris/s", "n_tris": n, "value": n / ms / 1e3,
+                 "unit": "Mtris/s", "ms": ms, "min_ms": float(np.min(times)), "builds": steps}
+
+
 def time_frames(ctx, torch, passes, frames, flush=None):
     """Device time (CUDA events on the context's stream) of `frames` renders
     of `passes` passes each, after one warm-up frame; L2 flushed before each
