@@ -75,6 +75,28 @@ def ncu_traffic(profile, key):
     return None
 
 
+def issue_roofline(profile):
+    """What bounds a latency- and SIMT-bound kernel: issue-active (share of
+    cycles an SM sub-partition issues) times active lanes per issued warp
+    instruction / 32, from the ncu summary under profiles/ (lines
+    `smsp__issue_active ... %` and `smsp__thread_inst_executed_per_inst_executed
+    ... of 32 lanes`); None when absent."""
+    act = lanes = None
+    try:
+        with open(os.path.join(ROOT, "profiles", profile)) as f:
+            for line in f:
+                if line.startswith("smsp__issue_active"):
+                    act = float(line.split()[-2]) / 100.0
+                elif line.startswith("smsp__thread_inst_executed_per_inst_executed"):
+                    lanes = float(line.split()[1])
+    except (OSError, ValueError, IndexError):
+        return None
+    if act is None or lanes is None:
+        return None
+    return {"issue_active": act, "lanes_per_instruction": lanes, "frac": act * lanes / 32.0,
+            "unit": "of lane-issue peak", "source": "profiles/" + profile}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -588,8 +610,9 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
     dev_ms = float(np.mean([m[0] for m in ms]))
     frame_wall = float(np.mean([m[1] for m in ms]))
     # plain: one context per scene, in turn; per scene also its rate when
-    # its frame fills the GPU (1024x1024, one pass: 8x the lanes the GPU
-    # holds), the best any schedule can do for that scene's samples
+    # its frame fills the GPU (1024x1024 -- 7x the lanes the GPU holds --
+    # with the scene's own passes per pixel), the best any schedule can do
+    # for that scene's samples
     plain_dev_ms, plain_wall = 0.0, 0.0
     table = []
     for (sh, lc, cam), sp, sd in zip(data, specs, seeds):
@@ -611,17 +634,20 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
         plain_dev_ms += scene_ms
         plain_wall += time.perf_counter() - t1
         ctx.close()
-        full = pt.Context(1024, 1024, accel=abi.ACCEL_BVH)
-        full.set_shapes(sh, lc)
-        full.build(abi.ACCEL_BVH, BUILD_FLAGS)
-        full.set_camera(cam)
-        full.set_seeds(pt.make_seeds(5000, 2 * 1024 * 1024))
-        full_ms = time_frames(full, torch, 1, 1)
-        full.close()
         s_i = sp["res"] * sp["res"] * sp["spp"]
+        if sp["res"] >= 1024:
+            full_msps = s_i / scene_ms / 1e3
+        else:
+            full = pt.Context(1024, 1024, accel=abi.ACCEL_BVH)
+            full.set_shapes(sh, lc)
+            full.build(abi.ACCEL_BVH, BUILD_FLAGS)
+            full.set_camera(cam)
+            full.set_seeds(pt.make_seeds(5000, 2 * 1024 * 1024))
+            full_ms = time_frames(full, torch, sp["spp"], 1)
+            full.close()
+            full_msps = 1024 * 1024 * sp["spp"] / full_ms / 1e3
         table.append({"shapes": int(len(sh)), "res": sp["res"], "spp": sp["spp"], "samples": s_i,
-                      "plain_ms": scene_ms, "plain_msps": s_i / scene_ms / 1e3,
-                      "full_msps": 1024 * 1024 / full_ms / 1e3})
+                      "plain_ms": scene_ms, "plain_msps": s_i / scene_ms / 1e3, "full_msps": full_msps})
     return data, specs, {"metric": "Msamples/s", "unit": "Msamples/s",
             "workload": "64 scenes, master seed 7: %d shapes, %.1f M samples per frame, depth 6"
                         % (shapes_total, samples / 1e6),
@@ -633,7 +659,7 @@ def bench_batched(pt, abi, scenes, torch, frames=2):
                                 "upload, build, render, pixels"},
             "ceiling": {"speedup": plain_dev_ms / sum(r["samples"] / r["full_msps"] / 1e3 for r in table),
                         "how": "sum of plain per-scene render ms / sum of (scene samples / that scene's "
-                               "rate on a 1024x1024 one-pass frame, which fills the GPU)",
+                               "rate on a 1024x1024 frame of its own passes, which fills the GPU)",
                         "small_scene_share": float(sum(r["samples"] for r in table if r["samples"] < 1 << 20))
                                              / samples},
             "per_scene": table,
@@ -771,7 +797,9 @@ def main():
                          "traffic": ncu_traffic("k_render_icosphere81934_512x512_16spp.txt",
                                                 "traffic_bytes_per_launch"),
                          "peak_kind": peak_kind, "kernel": "k_render",
-                         "model": "per query 32 B + 60 B/node visit + 36 B/prim test, GPU-counted",
+                         "model": "bytes touched (L1/L2-served), not DRAM: per query 32 B + 60 B/node "
+                                  "visit + 36 B/prim test, GPU-counted",
+                         "issue": issue_roofline("k_render_icosphere81934_512x512_16spp.txt"),
                          "bytes_per_frame": bytes_frame,
                          "counts": {"ext_queries": ext_q, "shadow_queries": sh_q,
                                     "ext_node_visits": ext_v, "ext_prim_tests": ext_p,
