@@ -1915,21 +1915,6 @@ cudaError_t launch_treelet(ptgpu_bvh_node *btn, ptgpu_bvh_node *btl, int n, int 
 // installed by the caller or restructured by the treelet pass): a child is a
 // leaf when nLeft == min / nRight == max.
 // ---------------------------------------------------------------------------
-// PTGPU_LEAF_PAIRS: a child node whose two children are leaves next to each
-// other in leaf order is referenced from its parent as a leaf range of those
-// two primitives (its box stays the child's box), so a walk tests both
-// primitives without a step for the child node.  The primitives a ray tests
-// can only grow (never fewer: the pair is tested whenever its box is
-// entered), and the primitive order inside the range is leaf order, so
-// closest hits, their tie rule and shadow answers are unchanged.
-#ifndef PTGPU_LEAF_PAIRS
-#define PTGPU_LEAF_PAIRS 0
-#endif
-__device__ __forceinline__ bool leaf_pair(const ptgpu_bvh_node &c, int n) {
-    return c.nLeft == c.min && c.nRight == c.max && c.nLeft >= 0 && c.nRight == c.nLeft + 1 &&
-           c.nRight < n;
-}
-
 __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
                                const ptgpu_bvh_node *__restrict__ btl, int n,
                                const float4 *__restrict__ prims0, float4 *__restrict__ nodes,
@@ -1956,16 +1941,6 @@ __global__ void k_abi_to_trace(const ptgpu_bvh_node *__restrict__ btn,
         o[2] = make_float4(rb.min_y, rb.max_y, rb.min_z, rb.max_z);
         int4 q = make_int4((ll ? shape_base : node_base) + li, (rl ? shape_base : node_base) + ri,
                            ll ? 1 : 0, rl ? 1 : 0);
-        if (PTGPU_LEAF_PAIRS) {
-            if (!ll) {
-                const ptgpu_bvh_node c = btn[li];
-                if (leaf_pair(c, n)) { q.x = shape_base + c.nLeft; q.z = 2; }
-            }
-            if (!rl) {
-                const ptgpu_bvh_node c = btn[ri];
-                if (leaf_pair(c, n)) { q.y = shape_base + c.nLeft; q.w = 2; }
-            }
-        }
         o[3] = *reinterpret_cast<float4 *>(&q);
     }
 }
