@@ -357,7 +357,7 @@ static int ptgpu_get_shapes_body(ptgpu_ctx *c, ptgpu_shape *out, uint32_t n) {
             CK(c->d_export.ensure((size_t)n * sizeof(ptgpu_shape)));
             CK(launch_export_shapes(c->d_shapes.as<ptgpu_shape>(), c->d_export.as<ptgpu_shape>(),
                                     c->d_verts.as<float>(), c->d_type.as<uint8_t>(), c->d_keys.as<uint32_t>(),
-                                    c->d_aabbs.as<float4>(), (int)n, c->stream));
+                                    (int)n, c->stream));
             c->shapes_exported = true;
             c->export_ready = true;
         }

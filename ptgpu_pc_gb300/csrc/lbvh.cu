@@ -23,7 +23,6 @@
 #include <cfloat>
 #include <cstring>
 #include <cstdint>
-#include <atomic>
 #include <mutex>
 #include <cuda_runtime.h>
 
@@ -230,13 +229,6 @@ __device__ __forceinline__ float4 ld_last_f4(const float4 *a) {
     return v;
 }
 
-// PTGPU_BUCKET_RECORDS=1: the bound records are written by k_morton_bucket,
-// grouped, instead of here in shape order (see k_morton_bucket)
-#ifndef PTGPU_BUCKET_RECORDS
-#define PTGPU_BUCKET_RECORDS 0
-#endif
-constexpr bool kBucketRecords = PTGPU_BUCKET_RECORDS != 0;
-
 // Centroid bounds, and each shape's bound stored as one aligned 32-byte
 // record for the later kernels (the emission kernel gathers it in sorted
 // order: one sector per leaf instead of a 36-byte vertex triple).
@@ -245,9 +237,7 @@ __device__ __forceinline__ void centroid_shape(const float *__restrict__ v, bool
                                                float4 *__restrict__ rec, float lo[3], float hi[3]) {
     float b[6];
     shape_bound(v, 0, tri, b);
-    if constexpr (kBucketRecords) {
-        // records come from k_morton_bucket
-    } else if constexpr (l2_hint(kL2BoundsLast)) {
+    if constexpr (l2_hint(kL2BoundsLast)) {
         st_last_f4(rec, make_float4(b[0], b[1], b[2], b[3]));
         st_last_f4(rec + 1, make_float4(b[4], b[5], 0.f, 0.f));
     } else {
@@ -489,139 +479,6 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
         for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x)
             if (s_hist[i]) atomicAdd(&st->hist[0][0] + i, s_hist[i]);
     }
-}
-
-// ---------------------------------------------------------------------------
-// Grouped bound records (PTGPU_BUCKET_RECORDS=1).  k_emit gathers each leaf's
-// bound record in sorted order.  With the records in shape order that gather
-// is random over the whole array, and every record costs DRAM accesses of its
-// own.  Here the records are written grouped by the key's top 6 bits instead
-// (the octree cell of the centroid two levels down), and the sort's values
-// are record positions, not shape ids.  The leaves of one group are
-// contiguous in sorted order, so at any time the emission reads the records of
-// a few groups only: a few MB that stay in L2, read from DRAM about once.
-//
-// k_morton_bucket makes each shape's bound from its vertices (k_centroid_bounds
-// then only reduces the centroid bounds and writes no records), its key and
-// the four digit histograms.  Each block of 256 shapes is then reordered by
-// group in shared memory, stably.  Its keys and 32-byte records (bound, shape
-// id) are written back into the block's own 256 slots in that order.  Equal
-// keys are in one group, and blocks hold shapes in index order. So
-// positions keep shape order among equal keys, and the stable sort by key
-// gives the same permutation as before.
-// ---------------------------------------------------------------------------
-constexpr int kGroups = 64;                 // ~key >> 24 is 192..255 for a 30-bit code
-
-// vertex buffers of k_morton_bucket: blocks are copied RING - 1 steps ahead
-#ifndef PTGPU_MB_RING
-#define PTGPU_MB_RING 3
-#endif
-constexpr int kMbRing = PTGPU_MB_RING;
-static_assert(kMbRing == 2 || kMbRing == 3, "two or three vertex buffers");
-
-__global__ void __launch_bounds__(256, kMbRing == 2 ? 8 : 6) k_morton_bucket(const float *__restrict__ verts,
-                                                           const uint8_t *__restrict__ type, int all_tri,
-                                                           int n, BuildState *st, uint32_t *__restrict__ keys,
-                                                           float4 *__restrict__ recs) {
-    pdl_begin();
-    __shared__ uint32_t s_hist[4 * 256];
-    __shared__ __align__(16) float s_v[kMbRing][256 * 9];   // blocks' vertices, a ring
-    __shared__ uint32_t s_wc[8][kGroups];               // per warp: group counts
-    __shared__ uint32_t s_wp[8][kGroups];               // per warp: group offsets in the block
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    for (int i = tid; i < 4 * 256; i += 256) s_hist[i] = 0u;
-    for (int i = tid; i < 8 * kGroups; i += 256) (&s_wc[0][0])[i] = 0u;
-    float lo[3], hi[3];
-    for (int a = 0; a < 3; ++a) { lo[a] = ord2f(st->cmin[a]); hi[a] = ord2f(st->cmax[a]); }
-    const bool aligned = (reinterpret_cast<uintptr_t>(verts) & 15) == 0;
-    const int nblocks = (n + 255) / 256;
-    // a whole block's 9216 bytes of vertices as 576 16-byte copies (blocks
-    // start on a 16-byte boundary: 256 * 36 bytes apart); a partial block is
-    // read directly
-    auto fetch = [&](int blk, int slot) {
-        if (aligned && blk >= 0 && (int64_t)(blk + 1) * 256 <= n) {
-            const float4 *src = reinterpret_cast<const float4 *>(verts + 9 * (size_t)blk * 256);
-            float4 *dst = reinterpret_cast<float4 *>(s_v[slot]);
-            for (int q = tid; q < 576; q += 256) cp_async16(dst + q, src + q);
-        }
-        cp_async_commit();
-    };
-    int blk = nblocks - 1 - (int)blockIdx.x;   // from the end: the tail is still in L2
-    for (int a = 0; a < kMbRing - 1; ++a) fetch(blk - a * (int)gridDim.x, a);
-    const unsigned lt_mask = (1u << lane) - 1u;
-    for (int it = 0; blk >= 0; ++it, blk -= gridDim.x) {
-        if (kMbRing == 2) cp_async_wait0(); else cp_async_wait1();
-        // this block's vertices have landed; the buffer read one step ago is free
-        __syncthreads();
-        fetch(blk - (kMbRing - 1) * (int)gridDim.x, (it + kMbRing - 1) % kMbRing);
-        const int i = blk * 256 + tid;
-        const bool valid = i < n;
-        const bool whole = aligned && (int64_t)(blk + 1) * 256 <= n;
-        float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        uint32_t key = 0u;
-        if (valid) {
-            const bool tri = all_tri || type[i] == PTGPU_TRIANGLE;
-            const float *v = whole ? s_v[it % kMbRing] + 9 * tid : verts + 9 * (size_t)i;
-            shape_bound(v, 0, tri, b);
-            // the same centroid as k_morton: the bound's centre, a sphere's centre
-            const f3 p = tri ? mk3((b[0] + b[1]) / 2.0f, (b[2] + b[3]) / 2.0f, (b[4] + b[5]) / 2.0f)
-                             : mk3(v[0], v[1], v[2]);
-            const uint32_t qa = quantise10(p.x, lo[0], hi[0]);
-            const uint32_t qb = quantise10(p.y, lo[1], hi[1]);
-            const uint32_t qc = quantise10(p.z, lo[2], hi[2]);
-            key = ~morton30(qa & 1023u, qb & 1023u, qc & 1023u);
-        }
-        count_digits(s_hist, key, valid, lane);
-        // stable grouping: rank among the warp's lanes of the same group,
-        // per-warp counts, offsets over (group, warp) in that order
-        const uint32_t g = (key >> 24) & (kGroups - 1);
-        const unsigned vm = __ballot_sync(0xffffffffu, valid);
-        const unsigned peers = __match_any_sync(0xffffffffu, valid ? g : 0xffffffffu) & vm;
-        const uint32_t r = (uint32_t)__popc(peers & lt_mask);
-        if (valid && r == 0u) s_wc[w][g] = (uint32_t)__popc(peers);
-        __syncthreads();
-        if (w == 0) {
-            // lane l: groups 2l and 2l+1 -- offsets over the warps (the
-            // counts are cleared as they are read), then the block-wide
-            // exclusive scan of the group totals
-            uint32_t t0 = 0u, t1 = 0u;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint32_t c0 = s_wc[k][2 * lane], c1 = s_wc[k][2 * lane + 1];
-                s_wc[k][2 * lane] = 0u;
-                s_wc[k][2 * lane + 1] = 0u;
-                s_wp[k][2 * lane] = t0;
-                s_wp[k][2 * lane + 1] = t1;
-                t0 += c0;
-                t1 += c1;
-            }
-            uint32_t x = t0 + t1;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            const uint32_t ex = x - t0 - t1;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                s_wp[k][2 * lane] += ex;
-                s_wp[k][2 * lane + 1] += ex + t0;
-            }
-        }
-        __syncthreads();
-        if (valid) {
-            // straight to the block's slots: a key and one whole 32-byte
-            // record per shape
-            const size_t pos = (size_t)blk * 256 + s_wp[w][g] + r;
-            keys[pos] = key;
-            recs[2 * pos] = make_float4(b[0], b[1], b[2], b[3]);
-            recs[2 * pos + 1] = make_float4(b[4], b[5], __int_as_float(i), 0.f);
-        }
-    }
-    cp_async_wait0();
-    __syncthreads();
-    for (int i = tid; i < 4 * 256; i += 256)
-        if (s_hist[i]) atomicAdd(&st->hist[0][0] + i, s_hist[i]);
 }
 
 // Digit histograms of all four passes.  Each thread counts runs of equal
@@ -1367,7 +1224,7 @@ static_assert(kEmitLeaves == kLeafThreads, "one leaf per thread");
 // window before its bound record, so the record's address is known when the
 // gather is issued (otherwise the index load's latency is waited out first)
 #ifndef PTGPU_EMIT_INDEX_AHEAD
-#define PTGPU_EMIT_INDEX_AHEAD 0
+#define PTGPU_EMIT_INDEX_AHEAD 1
 #endif
 // idx: the leaf's entry of `sorted`
 __device__ __forceinline__ void gather_bound(const float4 *__restrict__ aabbs, int idx, int n,
@@ -1375,8 +1232,6 @@ __device__ __forceinline__ void gather_bound(const float4 *__restrict__ aabbs, i
     sh = min(max(idx, 0), n - 1);   // in bounds even after a failed sort
     q0 = ld_hint_f4<kL2Gather>(aabbs + 2 * (size_t)sh);
     q1 = ld_hint_f4<kL2Gather>(aabbs + 2 * (size_t)sh + 1);
-    if constexpr (kBucketRecords)   // sorted holds record positions; the record holds the shape id
-        sh = min(max(__float_as_int(q1.z), 0), n - 1);
 }
 
 // stages the record of the block at `level` starting at leaf T0 + l0 into
@@ -2172,20 +2027,17 @@ __global__ void k_gather_prims(const int32_t *__restrict__ order, int count,
     prims[3 * (size_t)i + 2] = prims0[3 * (size_t)s + 2];
 }
 
-// Shape.b / index / morton_code as CLBVH::CLBVH leaves them in the shapes.
-// With grouped records the keys are in record order: thread j takes record
-// j's shape and key.
+// Shape.b / index / morton_code as CLBVH::CLBVH leaves them in the shapes
 __global__ void k_export_shapes(const ptgpu_shape *__restrict__ shapes, ptgpu_shape *__restrict__ out,
                                 const float *__restrict__ verts, const uint8_t *__restrict__ type,
-                                const uint32_t *__restrict__ keys, const float4 *__restrict__ recs, int n) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const int i = kBucketRecords ? min(max(__float_as_int(recs[2 * (size_t)j + 1].z), 0), n - 1) : j;
+                                const uint32_t *__restrict__ keys, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
     float b[6];
     shape_bound(verts, i, type[i] == PTGPU_TRIANGLE, b);
     ptgpu_shape s = shapes[i];
     s.index = i;
-    s.morton_code = ~keys[j];
+    s.morton_code = ~keys[i];
     s.b.min_x = b[0]; s.b.max_x = b[1];
     s.b.min_y = b[2]; s.b.max_y = b[3];
     s.b.min_z = b[4]; s.b.max_z = b[5];
@@ -2247,8 +2099,6 @@ static cudaError_t launch_chained(void (*k)(P...), int grid, int block, size_t s
 // shared-memory opt-ins of the build kernels, once per device; contexts,
 // batches, the server's worker and the no-allocation entry point may build
 // from different host threads at once, so the per-device flags are guarded
-static std::atomic<int> g_morton_bucket_ctas{1};   // resident k_morton_bucket CTAs per SM (set once)
-
 static cudaError_t launch_lbvh_prepare_attrs() {
     static std::mutex attr_mutex;
     static bool attr_set[64] = {false};
@@ -2264,11 +2114,6 @@ static cudaError_t launch_lbvh_prepare_attrs() {
     sort_attrs(k_onesweep<false, true, true>, smem);
     cudaFuncSetAttribute(k_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
     cudaFuncSetAttribute(k_tiles_seg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
-    if (kBucketRecords) {
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_morton_bucket, 256, 0) == cudaSuccess && nb > 0)
-            g_morton_bucket_ctas.store(nb, std::memory_order_relaxed);
-    }
     e = cudaGetLastError();
     if (e == cudaSuccess && dev >= 0 && dev < 64) attr_set[dev] = true;
     return e;
@@ -2294,13 +2139,7 @@ cudaError_t launch_lbvh_build(const LbvhBuffers &b, int n, int all_tri, int sm_c
 #ifndef PTGPU_MORTON_HIST
 #define PTGPU_MORTON_HIST 1
 #endif
-    if (kBucketRecords) {
-        // one wave of the resident CTAs: each walks the same number of blocks
-        const int mb_grid = grid_for(n, 256, sm_count * g_morton_bucket_ctas.load(std::memory_order_relaxed));
-        e = launch_chained(k_morton_bucket, mb_grid, 256, 0, s, (const float *)b.verts, (const uint8_t *)b.type,
-                           all_tri, n, b.state, b.keys, b.aabbs);
-        if (e != cudaSuccess) return e;
-    } else if (PTGPU_MORTON_HIST) {
+    if (PTGPU_MORTON_HIST) {
         e = launch_chained(k_morton<true>, red_grid, 256, 0, s, (const float *)b.verts, (const float4 *)b.aabbs,
                            (const uint8_t *)b.type, all_tri, n, b.state, b.keys);
         if (e != cudaSuccess) return e;
@@ -2403,10 +2242,9 @@ cudaError_t launch_gather_prims(const int32_t *order, int count, const float4 *p
 }
 
 cudaError_t launch_export_shapes(const ptgpu_shape *shapes, ptgpu_shape *out, const float *verts,
-                                 const uint8_t *type, const uint32_t *keys, const float4 *recs, int n,
-                                 cudaStream_t s) {
+                                 const uint8_t *type, const uint32_t *keys, int n, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_export_shapes<<<(n + 255) / 256, 256, 0, s>>>(shapes, out, verts, type, keys, recs, n);
+    k_export_shapes<<<(n + 255) / 256, 256, 0, s>>>(shapes, out, verts, type, keys, n);
     return cudaGetLastError();
 }
 

@@ -88,10 +88,8 @@ cudaError_t launch_collapse4(const float4 *nodes2, int n_int, float4 *nodes4, cu
 cudaError_t launch_gather_prims(const int32_t *order, int count, const float4 *prims0,
                                 float4 *prims, cudaStream_t s);
 // shapes with a BVH build's index / morton_code / b written into out
-// keys and recs: the build's key and bound-record arrays
 cudaError_t launch_export_shapes(const ptgpu_shape *shapes, ptgpu_shape *out, const float *verts,
-                                 const uint8_t *type, const uint32_t *keys, const float4 *recs, int n,
-                                 cudaStream_t s);
+                                 const uint8_t *type, const uint32_t *keys, int n, cudaStream_t s);
 
 // trace.cu
 // One scene of a batched render.  Node, primitive, material and light
