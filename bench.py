@@ -520,7 +520,7 @@ def served_requests(specs, n_req, rate, seed=5, hit=0.7):
     return out
 
 
-def bench_served(pt, abi, data, specs, rates=(10, 30, 100, 300, 1000), n_req=64):
+def bench_served(pt, abi, data, specs, rates=(10, 30, 100, 300, 1000), n_req=64, server_flags=0):
     """Requests arriving at each rate, served with continuous batching (one
     server, 120 GB budget, scenes resident under LRU) and, for comparison,
     by the plain path: one request after another, each building its scene in
@@ -531,7 +531,7 @@ def bench_served(pt, abi, data, specs, rates=(10, 30, 100, 300, 1000), n_req=64)
         reqs = served_requests(specs, n_req, rate)
         samples = float(sum(r["res"] * r["res"] * r["spp"] for r in reqs))
         # served
-        srv = pt.Server(budget_bytes=120 << 30)
+        srv = pt.Server(budget_bytes=120 << 30, flags=server_flags)
         ids = {}
         for r in reqs:
             if r["scene"] not in ids:
@@ -683,6 +683,11 @@ def main():
                     help="requests per arrival rate in the served leg")
     ap.add_argument("--served-only", action="store_true",
                     help="run only the batched and served legs (the full request sweep)")
+    ap.add_argument("--served-rates", default="10,30,100,300,1000",
+                    help="arrival rates (requests/s) of the served leg, comma-separated")
+    ap.add_argument("--served-policy", default="fill", choices=["fill", "all"],
+                    help="server steps: oldest requests up to one GPU filling (fill) or every "
+                         "admitted request (all)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -692,13 +697,16 @@ def main():
     import torch
     import ptgpu_pc_gb300 as pt
     from ptgpu_pc_gb300 import abi, scenes
+    served_rates = tuple(float(x) for x in args.served_rates.split(","))
+    server_flags = abi.SERVER_ALL_ACTIVE if args.served_policy == "all" else 0
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
     if args.served_only:
         # the batching leg and the full request sweep on their own (not a
         # benchmark line: the figures behind profiles/served_sweep.md)
         data, specs, batched = bench_batched(pt, abi, scenes, torch)
-        served = bench_served(pt, abi, data, specs, n_req=args.served_requests)
+        served = bench_served(pt, abi, data, specs, rates=served_rates, n_req=args.served_requests,
+                              server_flags=server_flags)
         print(json.dumps({"batched": batched, "served": served}), flush=True)
         return
 
@@ -831,7 +839,9 @@ def main():
         kd = bench_config2_kd(pt, abi, shapes, lc, cam, torch, flush)
         if not args.no_batched:
             data, specs, line["batched"] = bench_batched(pt, abi, scenes, torch)
-            line["served"] = bench_served(pt, abi, data, specs, n_req=args.served_requests)
+            line["served"] = bench_served(pt, abi, data, specs, rates=served_rates, n_req=args.served_requests,
+                                          server_flags=server_flags)
+            line["served_policy"] = args.served_policy
         if rank == 0:
             cref = CpuReference(shapes, lc, cam, target_s=args.ref_seconds)
             v, cores, desc, _ = cref.sample()

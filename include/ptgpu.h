@@ -352,8 +352,19 @@ typedef struct {
     int64_t shape_slots_used, pixel_slots_used, light_slots_used;
 } ptgpu_server_info;
 
+/* Steps.  By default each step renders the admitted requests oldest first
+ * while their pixels add up to at most one filling of the GPU (four pixels
+ * per resident render lane); the oldest is always rendered, the others wait
+ * for a later step.  A request that fills the GPU by itself then runs alone,
+ * as in a first-come queue, while small ones still share steps.  With this
+ * server flag every admitted request takes part in every step instead: a
+ * few percent more samples per second, but requests that arrive during a
+ * large one slow it down (a longer p99). */
+#define PTGPU_SERVER_ALL_ACTIVE  0x100
+
 int  ptgpu_server_create(int32_t device, int64_t budget_bytes, int32_t quantum, uint32_t flags,
-                         ptgpu_server **out);  /* flags: PTGPU_FLAG_ARGS_RTL; quantum 0 = 4 */
+                         ptgpu_server **out);  /* flags: PTGPU_FLAG_ARGS_RTL, PTGPU_SERVER_ALL_ACTIVE;
+                                                  quantum 0 = 4 */
 int  ptgpu_server_destroy(ptgpu_server *s);    /* finishes admitted work first */
 /* Registers a scene (copied); built on its first request with build_flags. */
 int  ptgpu_server_add_scene(ptgpu_server *s, const ptgpu_shape *shapes, uint32_t n,

@@ -114,6 +114,7 @@ FLAG_WAVEFRONT = 0x1
 FLAG_MORTON_DELTA = 0x2        # reserved: ptgpu_build answers E_INVAL
 FLAG_TREELET = 0x4
 FLAG_ARGS_RTL = 0x8
+SERVER_ALL_ACTIVE = 0x100
 FLAG_WIDE_TRAVERSAL = 0x10
 FLAG_KD_HOST = 0x20
 FLAG_ROW_ORDER = 0x40

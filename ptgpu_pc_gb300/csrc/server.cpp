@@ -11,8 +11,10 @@
 // its scene is resident or can be built, and its pixels fit, possibly after
 // evicting scenes no admitted request uses (least recently used first).
 //
-// Each step renders up to `quantum` passes of every admitted request (at
-// most 256 per launch) starting at the request's sample count, so a request
+// Each step renders up to `quantum` passes of the oldest admitted requests
+// whose pixels fit one filling of the GPU (or of every admitted request, with
+// PTGPU_SERVER_ALL_ACTIVE; at most 256 per launch) starting at the request's
+// sample count, so a request
 // refines progressively and new requests join at step boundaries.  The
 // running mean and the seeds are stored and reloaded between steps exactly
 // as the kernel keeps them in registers within one launch, so a request's
@@ -133,6 +135,7 @@ struct ptgpu_server {
     int device = 0;
     int64_t budget = 0;
     int quantum = 4;
+    bool fill_cap = true;      // false with PTGPU_SERVER_ALL_ACTIVE
     int rtl = 0;
     int sm_count = 1;
     cudaStream_t stream = nullptr;
@@ -542,18 +545,35 @@ void admit(ptgpu_server *s) {
     }
 }
 
-// One step: up to `quantum` passes of every admitted request, one launch.
+// One step: up to `quantum` passes of the oldest admitted requests whose
+// pixels fit one filling of the GPU (with PTGPU_SERVER_ALL_ACTIVE: of every
+// admitted request), one launch.
 int step(ptgpu_server *s) {
     drop_cancelled_active(s);
-    const int S = (int)s->active.size();
-    if (S == 0) return PTGPU_OK;
+    const int A = (int)s->active.size();
+    if (A == 0) return PTGPU_OK;
+    int depth = 0;
+    for (int k = 0; k < A; ++k) depth = std::max(depth, scene_of(s, s->active[k]->r.scene).depth);
+    // a binary traversal pushes at most two words per level
+    const int stack = render_stack_for_depth(depth);
+    const int grid = render_batch_grid(128, stack, 0);
+    // the requests of this step, oldest first (active is in admission order)
+    std::vector<int> sel;
+    const int64_t fill_px = (int64_t)grid * 128 * 4;
+    int64_t sel_px = 0;
+    for (int k = 0; k < A; ++k) {
+        const int64_t px = (int64_t)s->active[k]->r.width * s->active[k]->r.height;
+        if (!s->fill_cap || sel.empty() || sel_px + px <= fill_px) {
+            sel.push_back(k);
+            sel_px += px;
+        }
+    }
+    const int S = (int)sel.size();
     std::vector<BatchScene> recs(S);
     std::vector<int64_t> start(S + 1, 0);
-    int depth = 0;
     for (int k = 0; k < S; ++k) {
-        const Request &q = *s->active[k];
+        const Request &q = *s->active[sel[k]];
         const SceneEntry &sc = scene_of(s, q.r.scene);
-        depth = std::max(depth, sc.depth);
         BatchScene &r = recs[k];
         std::memset(&r, 0, sizeof(r));
         r.cam = q.r.camera;
@@ -595,9 +615,6 @@ int step(ptgpu_server *s) {
     a.scenes = s->d_recs.as<BatchScene>();
     a.pix_start = s->d_pix_start.as<int64_t>();
     a.n_scenes = S;
-    // a binary traversal pushes at most two words per level
-    const int stack = render_stack_for_depth(depth);
-    const int grid = render_batch_grid(128, stack, 0);
     SK(launch_render_batch(a, 128, stack, grid, s->stream));
     int32_t err = 0;
     SK(cudaMemcpyAsync(&err, s->d_err.p, sizeof(err), cudaMemcpyDeviceToHost, s->stream));
@@ -607,10 +624,16 @@ int step(ptgpu_server *s) {
         s->steps++;
     }
     std::vector<std::shared_ptr<Request>> keep;
-    for (int k = 0; k < S; ++k) {
+    for (int k = 0, j = 0; k < A; ++k) {
         std::shared_ptr<Request> q = s->active[k];
-        q->done_passes += recs[k].passes;
-        q->steps++;
+        if (j < S && sel[j] == k) {
+            q->done_passes += recs[j].passes;
+            q->steps++;
+            ++j;
+        } else {
+            keep.push_back(q);              // not in this step: waits for a later one
+            continue;
+        }
         if (q->done_passes < q->r.spp && !err) { keep.push_back(q); continue; }
         const int64_t px = (int64_t)q->r.width * q->r.height;
         q->pixels.resize(px);
@@ -684,6 +707,7 @@ int ptgpu_server_create(int32_t device, int64_t budget_bytes, int32_t quantum, u
     s->budget = budget_bytes;
     s->quantum = quantum ? quantum : 4;
     s->rtl = (flags & PTGPU_FLAG_ARGS_RTL) ? 1 : 0;
+    s->fill_cap = (flags & PTGPU_SERVER_ALL_ACTIVE) == 0;
     s->nodes.elem = 4 * sizeof(float4);
     s->prims.elem = 3 * sizeof(float4);
     s->prim_id.elem = sizeof(int32_t);

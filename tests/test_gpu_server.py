@@ -38,11 +38,11 @@ REQS = [(0, 48, 32, 5, 11), (1, 40, 40, 9, 12), (2, 32, 24, 3, 13), (3, 64, 48, 
         (0, 24, 24, 2, 15), (2, 16, 16, 12, 16)]
 
 
-@pytest.mark.parametrize("quantum", [1, 4])
-def test_served_results_equal_single_contexts_alone_and_mixed(quantum, built_lib):
+@pytest.mark.parametrize("quantum,flags", [(1, 0), (4, 0), (4, abi.SERVER_ALL_ACTIVE)])
+def test_served_results_equal_single_contexts_alone_and_mixed(quantum, flags, built_lib):
     import ptgpu_pc_gb300 as pt
     sc = _scenes()
-    with pt.Server(budget_bytes=8 << 30, quantum=quantum) as srv:
+    with pt.Server(budget_bytes=8 << 30, quantum=quantum, flags=flags) as srv:
         ids = [srv.add_scene(sh, lc, FLAGS) for sh, lc, _ in sc]
         # alone: one request at a time
         alone = []
@@ -107,3 +107,26 @@ def test_request_beyond_the_budget_is_rejected(built_lib):
         with pytest.raises(pt.PtgpuError) as e:
             srv.submit(99, cam, 8, 8, 1, 1)
         assert e.value.status == abi.E_INVAL
+
+
+def test_fill_cap_runs_a_gpu_filling_request_alone(built_lib):
+    """The default step policy: a request whose pixels fill the GPU by itself
+    (1536^2, over 15 pixels per resident lane) takes its steps alone, so the
+    small requests that arrive behind it wait and then share their own steps:
+    6 + 12 steps at quantum 1 (the largest small request has 12 passes).
+    Every result still equals the single-scene context's."""
+    import ptgpu_pc_gb300 as pt
+    sc = _scenes()
+    big = (0, 1536, 1536, 6, 21)
+    with pt.Server(budget_bytes=8 << 30, quantum=1) as srv:
+        ids = [srv.add_scene(sh, lc, FLAGS) for sh, lc, _ in sc]
+        reqs = [big] + REQS
+        tickets = [srv.submit(ids[s], sc[s][2], w, h, spp, seed) for s, w, h, spp, seed in reqs]
+        outs = [srv.wait(t) for t in tickets]
+        info = srv.info()
+    assert outs[0][2]["steps"] == big[3]
+    assert info["steps"] == big[3] + max(r[3] for r in REQS)
+    for (s, w, h, spp, seed), got in zip(reqs, outs):
+        px, col = _reference(sc[s][0], sc[s][1], sc[s][2], w, h, spp, seed)
+        assert np.array_equal(got[1].view(np.uint32), col.view(np.uint32)), (w, h, spp)
+        assert np.array_equal(got[0], px), (w, h, spp)
