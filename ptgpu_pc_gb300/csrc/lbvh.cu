@@ -669,6 +669,9 @@ constexpr int kLookback = PTGPU_LOOKBACK;   // predecessors read per look-back s
 #ifndef PTGPU_SORT_MINBLOCKS
 #define PTGPU_SORT_MINBLOCKS 3
 #endif
+#ifndef PTGPU_SKIP_EMPTY_DIGITS
+#define PTGPU_SKIP_EMPTY_DIGITS 1
+#endif
 
 // Look-back words are read and published with relaxed GPU-scope accesses:
 // each read sees the word as it is in L2, and several reads of one thread
@@ -931,7 +934,11 @@ __global__ void __launch_bounds__(kSortThreads, PTGPU_SORT_MINBLOCKS) k_onesweep
     uint32_t dstart = block_excl_scan256(count, sm.scan_tmp);
     if (dig_thread) {
         sm.digit_start[tid] = dstart;
-        const uint32_t excl = lookback_digit(status, tile, tid, count, st, sm.abort);
+        // a digit that no tile holds (its global count is 0: the last pass of
+        // 30-bit keys has 64 live digits of 256) needs no look-back; no tile
+        // publishes or reads its words
+        const bool live = !PTGPU_SKIP_EMPTY_DIGITS || gcount != 0u;
+        const uint32_t excl = live ? lookback_digit(status, tile, tid, count, st, sm.abort) : 0u;
         sm.tile_excl[tid] = goff + excl - dstart;   // + tile position = destination (mod 2^32)
     }
     __syncthreads();
