@@ -214,7 +214,6 @@ struct Trav {
     int cur, ccnt; // current item: internal node (ccnt == 0) or leaf range
     int sp;
     int any, hit;  // shadow query; a hit was found (shadow: occluded)
-    int skip;      // shadow query: the shape id it never tests
 };
 
 // Where a query starts: the root item, the scene's shape count and the shape
@@ -250,7 +249,6 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, const TraceRoot 
     q.prim = -1;
     q.tb = any ? maxt : kInfT;
     q.sp = 0;
-    q.skip = root.skip;
     const int n = root.n_shapes;
     if (n <= 0 || (any && n <= 1)) return true;
     if (tv.accel == PTGPU_ACCEL_NONE) {
@@ -287,15 +285,16 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, Trav &q, f3 o, f
 }
 
 // One item of the traversal: a leaf range's primitives or one node's
-// children.  Returns true when the query is answered.
+// children.  Returns true when the query is answered.  skip: the prim_id a
+// shadow query never tests (the scene's last shape, TraceRoot::skip).
 #ifndef PTGPU_TRAV_FUSE
 #define PTGPU_TRAV_FUSE 1
 #endif
 template <bool WIDE, bool COUNT, int STACK = kStackSize, class Stack>
-__device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, Stack &stack, Counts *cnt) {
+__device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, Stack &stack, Counts *cnt, int skip) {
     if (q.ccnt > 0) {
         for (int k = q.cur; k < q.cur + q.ccnt; ++k) {
-            if (q.any && __ldg(&tv.prim_id[k]) == q.skip) continue;
+            if (q.any && __ldg(&tv.prim_id[k]) == skip) continue;
             float dd = prim_intersect(tv.prims, k, q.o, q.d);
             if (COUNT) cnt->p++;
             if (dd != 0.f) {
@@ -402,7 +401,7 @@ __device__ __forceinline__ int trace_query(const TraceView &tv, f3 o, f3 d, bool
     Trav q;
     LocalStack<kStackSize> stack;
     if (!trav_begin<COUNT>(tv, q, o, d, any, maxt, cnt))
-        while (!trav_step<WIDE, COUNT>(tv, q, stack, cnt)) {}
+        while (!trav_step<WIDE, COUNT>(tv, q, stack, cnt, tv.n_shapes - 1)) {}
     t = any ? kInfT : q.tb;
     prim = q.prim;
     return q.hit;

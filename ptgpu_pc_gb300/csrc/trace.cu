@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
 #endif
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
-    q.any = 0; q.hit = 0; q.skip = -1;
+    q.any = 0; q.hit = 0;
+    int skip = a.tv.n_shapes - 1;   // the shape shadow queries never test (BATCH: the lane's scene's)
 #if PTGPU_RENDER_SHORT_STACK > 0
     // the bottom of each lane's traversal stack in shared memory, the rest in
     // local memory (ShortStack)
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
             root.n_shapes = __ldg(&S().n_shapes);
             root.skip = __ldg(&S().skip);
             root.box = S().root_box;
+            skip = root.skip;
         } else {
             root = view_root(a.tv);
         }
@@ -324,12 +326,12 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
             if (!busy) break;
             const unsigned live = __ballot_sync(0xffffffffu, state != ST_DONE);
             if (__popc(live & ~busy) * 32 >= refill * __popc(live)) break;
-            if (trav && trav_step<WIDE, COUNT, STACK>(a.tv, q, stack, cnt + q.any)) {
+            if (trav && trav_step<WIDE, COUNT, STACK>(a.tv, q, stack, cnt + q.any, skip)) {
                 trav = false;
                 fin = true;
             }
 #if PTGPU_RENDER_STEPS > 1
-            if (trav && trav_step<WIDE, COUNT, STACK>(a.tv, q, stack, cnt + q.any)) {
+            if (trav && trav_step<WIDE, COUNT, STACK>(a.tv, q, stack, cnt + q.any, skip)) {
                 trav = false;
                 fin = true;
             }
@@ -641,7 +643,7 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
     Counts cnt = {0, 0};
     const TraceRoot root = view_root(tv);
     Trav q;
-    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0; q.skip = -1;
+    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0;
 #if PTGPU_SHORT_STACK > 0
     __shared__ int s_stack[PTGPU_SHORT_STACK][128];
     ShortStack<kStackSize, PTGPU_SHORT_STACK, 128> stack;
@@ -679,7 +681,7 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
             if (!busy) break;
             const unsigned live = __ballot_sync(0xffffffffu, !done);
             if (__popc(live & ~busy) * 32 >= refill * __popc(live)) break;
-            if (trav && trav_step<WIDE, COUNT>(tv, q, stack, COUNT ? &cnt : nullptr)) {
+            if (trav && trav_step<WIDE, COUNT>(tv, q, stack, COUNT ? &cnt : nullptr, -1)) {   // closest only
                 trav = false;
                 fin = true;
             }
