@@ -62,7 +62,10 @@ enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 #define PTGPU_RENDER_SMEM_STATE 1   // 72 -> 64 registers, 8 CTAs per SM: 28.73 -> 28.58 ms per frame
 #endif
 #ifndef PTGPU_RENDER_MINBLOCKS
-#define PTGPU_RENDER_MINBLOCKS 7   // at least 7 CTAs of 128 lanes per SM (8 at 64 registers)
+// 8 CTAs of 128 lanes per SM, at most 64 registers (no spills); against 7:
+// 28.80 vs 28.88 ms per benchmark frame, 260.4 vs 275.5 ms per 16-scene
+// batched frame
+#define PTGPU_RENDER_MINBLOCKS 8
 #endif
 // A warp leaves its traversal steps to shade when at least this many 32nds
 // of its live lanes wait without a query in flight (32: when every query of
