@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
 #endif
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
-    q.any = 0; q.hit = 0;
+    q.any = 0;
     int skip = a.tv.n_shapes - 1;   // the shape shadow queries never test (BATCH: the lane's scene's)
 #if PTGPU_RENDER_SHORT_STACK > 0
     // the bottom of each lane's traversal stack in shared memory, the rest in
@@ -345,9 +345,9 @@ __global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const Re
         if (fin) {
             fin = false;
             if (q.any) {
-                if (!q.hit) ld = add3(ld, pend);
+                if (q.prim < 0) ld = add3(ld, pend);
                 ++li;
-            } else if (!q.hit) {
+            } else if (q.prim < 0) {
                 // RadianceOnePathTracing (rendering_kernel.cl:495-753)
                 state = -1;
             } else {
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
     Counts cnt = {0, 0};
     const TraceRoot root = view_root(tv);
     Trav q;
-    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0;
+    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0;
 #if PTGPU_SHORT_STACK > 0
     __shared__ int s_stack[PTGPU_SHORT_STACK][128];
     ShortStack<kStackSize, PTGPU_SHORT_STACK, 128> stack;
@@ -692,8 +692,8 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
         if (fin) {
             fin = false;
             tout[ray] = q.tb;
-            idout[ray] = (q.hit && q.prim >= 0) ? (uint32_t)__ldg(&tv.prim_id[q.prim]) : 0u;
-            hitout[ray] = q.hit;
+            idout[ray] = q.prim >= 0 ? (uint32_t)__ldg(&tv.prim_id[q.prim]) : 0u;
+            hitout[ray] = q.prim >= 0 ? 1 : 0;
         }
     }
     if (COUNT) {
