@@ -64,8 +64,13 @@ enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 #ifndef PTGPU_RENDER_MINBLOCKS
 // 8 CTAs of 128 lanes per SM, at most 64 registers (no spills); against 7:
 // 28.80 vs 28.88 ms per benchmark frame, 260.4 vs 275.5 ms per 16-scene
-// batched frame
+// batched frame; 9 (56 registers, 60 bytes spilled): 29.60 vs 28.75 ms
 #define PTGPU_RENDER_MINBLOCKS 8
+#endif
+#ifndef PTGPU_RENDER_BATCH_MINBLOCKS
+// the batched tracer at 9 CTAs per SM (56 registers, 96 bytes spilled): a
+// 16-scene batched frame 251.3 against 258.5 ms at 8
+#define PTGPU_RENDER_BATCH_MINBLOCKS 9
 #endif
 // A warp leaves its traversal steps to shade when at least this many 32nds
 // of its live lanes wait without a query in flight (32: when every query of
@@ -83,7 +88,7 @@ enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 constexpr int kMaxBatchScenes = 256;
 
 template <bool WIDE, bool COUNT, bool BATCH, int STACK>
-__global__ void __launch_bounds__(128, PTGPU_RENDER_MINBLOCKS) k_render(const RenderArgs a, unsigned int *pixel_counter) {
+__global__ void __launch_bounds__(128, BATCH ? PTGPU_RENDER_BATCH_MINBLOCKS : PTGPU_RENDER_MINBLOCKS) k_render(const RenderArgs a, unsigned int *pixel_counter) {
     __shared__ int64_t s_start[BATCH ? kMaxBatchScenes + 1 : 1];
     int64_t npx;
     if (BATCH) {
