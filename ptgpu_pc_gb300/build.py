@@ -16,7 +16,7 @@ CU_SOURCES = ["lbvh.cu", "trace.cu", "wavefront.cu", "noalloc.cu", "batch.cu", "
               "image.cu"]
 CPP_SOURCES = ["api.cpp", "kdtree.cpp", "loader.cpp", "batch.cpp", "server.cpp"]
 HEADERS = ["device.cuh", "types.h", "lbvh.h", "lbvh_topo.cuh", "host.h", "devbuf.h", "ingest.h",
-           "range_alloc.h"]
+           "range_alloc.h", "step_policy.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no contraction, so float results round like the reference's

@@ -43,6 +43,7 @@
 #include "ingest.h"
 #include "lbvh.h"
 #include "range_alloc.h"
+#include "step_policy.h"
 
 using namespace ptgpu;
 
@@ -558,16 +559,9 @@ int step(ptgpu_server *s) {
     const int stack = render_stack_for_depth(depth);
     const int grid = render_batch_grid(128, stack, 0);
     // the requests of this step, oldest first (active is in admission order)
-    std::vector<int> sel;
-    const int64_t fill_px = (int64_t)grid * 128 * 4;
-    int64_t sel_px = 0;
-    for (int k = 0; k < A; ++k) {
-        const int64_t px = (int64_t)s->active[k]->r.width * s->active[k]->r.height;
-        if (!s->fill_cap || sel.empty() || sel_px + px <= fill_px) {
-            sel.push_back(k);
-            sel_px += px;
-        }
-    }
+    std::vector<int64_t> px(A);
+    for (int k = 0; k < A; ++k) px[k] = (int64_t)s->active[k]->r.width * s->active[k]->r.height;
+    const std::vector<int> sel = step_selection(px, s->fill_cap, (int64_t)grid * 128 * 4);
     const int S = (int)sel.size();
     std::vector<BatchScene> recs(S);
     std::vector<int64_t> start(S + 1, 0);

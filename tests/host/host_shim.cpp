@@ -1,6 +1,6 @@
 // host_shim.cpp -- test-only C entry points over the library's host code
 // (KD-tree build, scene loader, camera, closed-form LBVH topology, the
-// server's slot allocator), compiled
+// server's slot allocator and step policy), compiled
 // without CUDA by the CPU tests.
 #include <algorithm>
 #include <cstdint>
@@ -14,6 +14,7 @@
 #include "../../ptgpu_pc_gb300/csrc/lbvh_topo.cuh"
 #include "../../ptgpu_pc_gb300/csrc/host.h"
 #include "../../ptgpu_pc_gb300/csrc/range_alloc.h"
+#include "../../ptgpu_pc_gb300/csrc/step_policy.h"
 
 extern "C" {
 
@@ -154,6 +155,14 @@ int shim_ra_free(void *a, int64_t *out, int max_pairs) {
         ++k;
     }
     return k;
+}
+
+// the serving step's request selection: indices into px (oldest first) into
+// out; returns their count
+int shim_step_selection(const int64_t *px, int n, int fill_cap, int64_t fill_px, int *out) {
+    const std::vector<int> sel = ptgpu::step_selection(std::vector<int64_t>(px, px + n), fill_cap != 0, fill_px);
+    for (size_t i = 0; i < sel.size(); ++i) out[i] = sel[i];
+    return (int)sel.size();
 }
 
 }

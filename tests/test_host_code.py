@@ -48,6 +48,7 @@ def shim(tmp_path_factory):
     L.shim_read_scene_compact.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, vp, vp]
     L.shim_compact_get.argtypes = [vp]
     L.shim_make_seeds.argtypes = [ctypes.c_uint64, vp, ctypes.c_uint32]
+    L.shim_step_selection.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, vp]
     return L
 
 
@@ -357,3 +358,40 @@ def test_server_slot_allocator_first_fit(shim):
         assert k == 1 and tuple(out[:2]) == (0, len(busy)) and shim.shim_ra_used(a) == 0
     finally:
         shim.shim_ra_delete(a)
+
+
+def _step(shim, px, fill_cap, fill_px):
+    a = np.asarray(px, np.int64)
+    out = np.zeros(max(len(a), 1), np.int32)
+    k = shim.shim_step_selection(_p(a), len(a), int(fill_cap), fill_px, _p(out))
+    return out[:k].tolist()
+
+
+def test_step_selection_fill_cap(shim):
+    """The server's step policy (step_policy.h): without a cap every admitted
+    request; with one, oldest first while the pixels fit, the oldest always
+    (even alone over the cap), and younger ones that fit after an older one
+    did not."""
+    cap = 700_000
+    big, mid, small = 1024 * 1024, 512 * 512, 128 * 128
+    assert _step(shim, [big, small, mid], False, cap) == [0, 1, 2]
+    assert _step(shim, [big, small, mid], True, cap) == [0]
+    assert _step(shim, [small, big, mid], True, cap) == [0, 2]
+    assert _step(shim, [mid, mid, mid], True, cap) == [0, 1]
+    assert _step(shim, [small] * 5, True, cap) == [0, 1, 2, 3, 4]
+    assert _step(shim, [], True, cap) == []
+    assert _step(shim, [cap], True, cap) == [0]
+    assert _step(shim, [cap - 1, 1, 1], True, cap) == [0, 1]
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        px = rng.choice([small, 256 * 256, mid, big], size=rng.integers(1, 12)).tolist()
+        sel = _step(shim, px, True, cap)
+        assert sel[0] == 0 and sel == sorted(sel)
+        assert sum(px[i] for i in sel[1:]) + px[0] <= max(cap, px[0]) or len(sel) == 1
+        # first fit: every request left out would not have fitted when it was reached
+        total = 0
+        for i, p in enumerate(px):
+            if i in sel:
+                total += p
+            else:
+                assert total + p > cap
