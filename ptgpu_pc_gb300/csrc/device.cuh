@@ -210,12 +210,12 @@ struct ShortStack {
 struct Trav {
     f3 o, d, inv;
     float tb;      // closest: best t so far; shadow: maxt
-    int prim;      // closest: traversal-order index of the best hit; shadow: 0 once
-                   // occluded.  A query has hit when prim >= 0 (the reference's
-                   // Intersect returns t < inf: a recorded hit)
+    int prim;      // closest: traversal-order index of the best hit
     int cur, ccnt; // current item: internal node (ccnt == 0) or leaf range
     int sp;
-    int any;       // shadow query
+    int any, hit;  // shadow query; a hit was found (shadow: occluded).  In the
+                   // BVH and KD walks any intersection sets it, recorded or not
+                   // (rendering_kernel.cl `intersected = 1`); brute force: t < inf
 };
 
 // Where a query starts: the root item, the scene's shape count and the shape
@@ -247,6 +247,7 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, const TraceRoot 
     q.o = o;
     q.d = d;
     q.any = any;
+    q.hit = 0;
     q.prim = -1;
     q.tb = any ? maxt : kInfT;
     q.sp = 0;
@@ -257,7 +258,7 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, const TraceRoot 
             for (int i = n - 2; i >= 0; --i) {
                 float dd = prim_intersect(tv.prims, i, o, d);
                 if (COUNT) cnt->p++;
-                if (dd != 0.f && dd < maxt) { q.prim = 0; return true; }
+                if (dd != 0.f && dd < maxt) { q.hit = 1; return true; }
             }
             return true;
         }
@@ -266,6 +267,7 @@ __device__ __forceinline__ bool trav_begin(const TraceView &tv, const TraceRoot 
             if (COUNT) cnt->p++;
             if (dd != 0.f && dd < q.tb) { q.tb = dd; q.prim = i; }
         }
+        q.hit = q.tb < kInfT;
         return true;
     }
     q.inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
@@ -299,8 +301,9 @@ __device__ __forceinline__ bool trav_step(const TraceView &tv, Trav &q, Stack &s
             if (COUNT) cnt->p++;
             if (dd != 0.f) {
                 if (q.any) {
-                    if (dd < q.tb) { q.prim = 0; return true; }
+                    if (dd < q.tb) { q.hit = 1; return true; }
                 } else {
+                    q.hit = 1;
                     // equal t: the lower traversal-order index wins, which in
                     // the BVH is the leaf the reference's left-first walk
                     // meets first (its `d < t` keeps the first one found)
@@ -403,7 +406,7 @@ __device__ __forceinline__ int trace_query(const TraceView &tv, f3 o, f3 d, bool
         while (!trav_step<WIDE, COUNT>(tv, q, stack, cnt, tv.n_shapes - 1)) {}
     t = any ? kInfT : q.tb;
     prim = q.prim;
-    return q.prim >= 0;
+    return q.hit;
 }
 
 }  // namespace ptgpu

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(128, BATCH ? PTGPU_RENDER_BATCH_MINBLOCKS : PT
 #endif
     Trav q;
     q.o = col; q.d = col; q.inv = col; q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0;
-    q.any = 0;
+    q.any = 0; q.hit = 0;
     int skip = a.tv.n_shapes - 1;   // the shape shadow queries never test (BATCH: the lane's scene's)
 #if PTGPU_RENDER_SHORT_STACK > 0
     // the bottom of each lane's traversal stack in shared memory, the rest in
@@ -350,9 +350,9 @@ __global__ void __launch_bounds__(128, BATCH ? PTGPU_RENDER_BATCH_MINBLOCKS : PT
         if (fin) {
             fin = false;
             if (q.any) {
-                if (q.prim < 0) ld = add3(ld, pend);
+                if (!q.hit) ld = add3(ld, pend);
                 ++li;
-            } else if (q.prim < 0) {
+            } else if (!q.hit) {
                 // RadianceOnePathTracing (rendering_kernel.cl:495-753)
                 state = -1;
             } else {
@@ -651,7 +651,7 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
     Counts cnt = {0, 0};
     const TraceRoot root = view_root(tv);
     Trav q;
-    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0;
+    q.tb = 0.f; q.prim = -1; q.cur = 0; q.ccnt = 0; q.sp = 0; q.any = 0; q.hit = 0;
 #if PTGPU_SHORT_STACK > 0
     __shared__ int s_stack[PTGPU_SHORT_STACK][128];
     ShortStack<kStackSize, PTGPU_SHORT_STACK, 128> stack;
@@ -697,8 +697,8 @@ __global__ void __launch_bounds__(128, WIDE ? 1 : PTGPU_CLOSEST_MINBLOCKS) k_tra
         if (fin) {
             fin = false;
             tout[ray] = q.tb;
-            idout[ray] = q.prim >= 0 ? (uint32_t)__ldg(&tv.prim_id[q.prim]) : 0u;
-            hitout[ray] = q.prim >= 0 ? 1 : 0;
+            idout[ray] = (q.hit && q.prim >= 0) ? (uint32_t)__ldg(&tv.prim_id[q.prim]) : 0u;
+            hitout[ray] = q.hit;
         }
     }
     if (COUNT) {
