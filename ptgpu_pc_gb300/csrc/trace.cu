@@ -68,8 +68,8 @@ enum : int { ST_NEED = 0, ST_GEN = 1, ST_EXT = 2, ST_NEE = 3, ST_DONE = 4 };
 #define PTGPU_RENDER_MINBLOCKS 8
 #endif
 #ifndef PTGPU_RENDER_BATCH_MINBLOCKS
-// the batched tracer at 9 CTAs per SM (56 registers, 96 bytes spilled): a
-// 16-scene batched frame 251.3 against 258.5 ms at 8
+// the batched tracer at 9 CTAs per SM (56 registers, 124 bytes spilled): a
+// 16-scene batched frame 252.6 against 260.4 ms at 8
 #define PTGPU_RENDER_BATCH_MINBLOCKS 9
 #endif
 // A warp leaves its traversal steps to shade when at least this many 32nds
