@@ -5,6 +5,7 @@
     python -m ptgpu_pc_gb300.cases closest [--n 4194304 --rays 16777216 --reps 2]
     python -m ptgpu_pc_gb300.cases batch   [--scenes 16 --tri-max 200000 --frames 2]
     python -m ptgpu_pc_gb300.cases kd      [--builds 2]
+    python -m ptgpu_pc_gb300.cases scene_build [--builds 2 --sweeps 2]
     python -m ptgpu_pc_gb300.cases ingest  [--n 1000000 --reps 2]
 
 render: the displaced-icosphere scene (81,934 shapes) built with `sweeps` treelet rounds,
@@ -44,6 +45,15 @@ def run_render(a):
             ctx.synchronize()
             print("render %dx%d %d spp frame %d: %.2f ms (host clock)"
                   % (a.width, a.height, a.spp, i, (time.perf_counter() - t0) * 1e3))
+
+
+def run_scene_build(a):
+    shapes, lc, _ = scenes.icosphere_scene(level=6)
+    with pt.Context(8, 8) as ctx:
+        ctx.set_shapes(shapes, lc)
+        for i in range(a.builds):
+            ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET | abi.treelet_sweeps(a.sweeps))
+            print("scene build %d (%d treelet rounds): %.3f ms" % (i, a.sweeps, ctx.last_build_ms()))
 
 
 def run_lbvh(a):
@@ -115,7 +125,7 @@ def run_ingest(a):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["render", "lbvh", "closest", "batch", "kd", "ingest"])
+    ap.add_argument("case", choices=["render", "lbvh", "closest", "batch", "kd", "ingest", "scene_build"])
     ap.add_argument("--width", type=int, default=512)
     ap.add_argument("--height", type=int, default=512)
     ap.add_argument("--spp", type=int, default=16)
@@ -133,6 +143,7 @@ def main():
     if a.case == "ingest" and a.n == 1 << 22:
         a.n = 1_000_000
     {"render": run_render, "lbvh": run_lbvh, "closest": run_closest, "batch": run_batch, "kd": run_kd,
+     "scene_build": run_scene_build,
      "ingest": run_ingest}[a.case](a)
 
 
