@@ -723,10 +723,12 @@ cudaError_t launch_trace_closest(const TraceView &tv, const ptgpu_ray *rays, int
     int grid = resident_grid(k, 128, 0);
     const int need = (n + 127) / 128;
     if (grid <= 0 || grid > need) grid = need;
-    // the closest-hit lanes refill earlier than the render's (20 of 32: 22
-    // measured 735 -> 695 Mrays/s on 2^24 rays against 4M triangles)
+    // the closest-hit lanes refill much earlier than the render's, whose
+    // refill also shades: a warp takes new rays once 8 of 32 live lanes are
+    // done (2^24 rays against 4M triangles: 16.76 ms at 8, 16.82 at 10, 16.95
+    // at 6, 16.99 at 12, 18.71 at 20, 21.11 at 24)
 #ifndef PTGPU_CLOSEST_REFILL
-#define PTGPU_CLOSEST_REFILL 20
+#define PTGPU_CLOSEST_REFILL 8
 #endif
     const int r = PTGPU_CLOSEST_REFILL;
     if (stats) {
