@@ -1,6 +1,6 @@
 """Fixed, seeded workloads of the hot path for profiling one kernel at a time.
 
-    python -m ptgpu_pc_gb300.cases render  [--width 512 --height 512 --spp 16 --frames 2 --flags 0 --sweeps 2]
+    python -m ptgpu_pc_gb300.cases render  [--width 512 --height 512 --spp 16 --frames 2 --flags 0 --sweeps 2 --accel bvh|kd]
     python -m ptgpu_pc_gb300.cases lbvh    [--n 4194304 --builds 2]
     python -m ptgpu_pc_gb300.cases closest [--n 4194304 --rays 16777216 --reps 2]
     python -m ptgpu_pc_gb300.cases batch   [--scenes 16 --tri-max 200000 --frames 2]
@@ -31,10 +31,14 @@ from ptgpu_pc_gb300 import abi, scenes
 
 def run_render(a):
     shapes, lc, cam = scenes.icosphere_scene(level=6)
-    with pt.Context(a.width, a.height, accel=abi.ACCEL_BVH, max_depth=a.max_depth,
+    accel = abi.ACCEL_KDTREE if a.accel == "kd" else abi.ACCEL_BVH
+    with pt.Context(a.width, a.height, accel=accel, max_depth=a.max_depth,
                     flags=a.flags) as ctx:
         ctx.set_shapes(shapes, lc)
-        ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET | abi.treelet_sweeps(a.sweeps))
+        if accel == abi.ACCEL_KDTREE:
+            ctx.build(abi.ACCEL_KDTREE)
+        else:
+            ctx.build(abi.ACCEL_BVH, abi.FLAG_TREELET | abi.treelet_sweeps(a.sweeps))
         print("scene build %.3f ms" % ctx.last_build_ms())
         ctx.set_camera(cam)
         ctx.set_seeds(pt.make_seeds(1, 2 * a.width * a.height))
@@ -133,6 +137,7 @@ def main():
     ap.add_argument("--frames", type=int, default=2)
     ap.add_argument("--flags", type=int, default=0, help="ptgpu_config.flags of the render context")
     ap.add_argument("--sweeps", type=int, default=2, help="treelet rounds of the scene build")
+    ap.add_argument("--accel", default="bvh", choices=["bvh", "kd"], help="render: the tree traversed")
     ap.add_argument("--n", type=int, default=1 << 22)
     ap.add_argument("--builds", type=int, default=2)
     ap.add_argument("--rays", type=int, default=1 << 24)
