@@ -1749,7 +1749,12 @@ constexpr int kTreeletThreads = 128;
 __device__ __forceinline__ int treelet_leaf(int lane, int lpw) {
     return lane < lpw ? (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * lpw + lane : 0x7fffffff;
 }
-static int treelet_lpw(int64_t leaves) { return leaves < (1 << 20) ? 16 : 32; }
+#ifndef PTGPU_TREELET_LPW
+#define PTGPU_TREELET_LPW 0    // leaves a warp climbs from; 0: 16 below 2^20 leaves, else 32
+#endif
+static int treelet_lpw(int64_t leaves) {
+    return PTGPU_TREELET_LPW > 0 ? PTGPU_TREELET_LPW : (leaves < (1 << 20) ? 16 : 32);
+}
 static int treelet_grid(int64_t leaves, int lpw) {
     return (int)((leaves + (int64_t)lpw * (kTreeletThreads / 32) - 1) / ((int64_t)lpw * (kTreeletThreads / 32)));
 }
